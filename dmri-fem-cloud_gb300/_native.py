@@ -1,0 +1,250 @@
+"""ctypes binding of libbtgpu.so (the C ABI declared in include/btgpu.h).
+
+The library is the only compute path: when it is missing or cannot be loaded
+every call raises, there is no CPU fallback.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbtgpu.so")
+
+BT_OK = 0
+BT_ERR_INVALID = 1
+BT_ERR_CUDA = 2
+BT_ERR_OOM = 3
+BT_ERR_NOT_CONVERGED = 4
+BT_ERR_BREAKDOWN = 5
+BT_ERR_TIMEOUT = 6
+BT_ERR_STATE = 7
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+MATRICES = {"M": 0, "K": 1, "T": 2, "R": 3, "Jx": 4, "Jy": 5, "Jz": 6}
+_ERRNAMES = {1: "BT_ERR_INVALID", 2: "BT_ERR_CUDA", 3: "BT_ERR_OOM", 4: "BT_ERR_NOT_CONVERGED",
+             5: "BT_ERR_BREAKDOWN", 6: "BT_ERR_TIMEOUT", 7: "BT_ERR_STATE"}
+
+# every function declared in include/btgpu.h
+EXPORTS = [
+    "bt_version", "bt_create", "bt_destroy", "bt_last_error", "bt_set_stream",
+    "bt_mesh_upload", "bt_mesh_info", "bt_set_coefficients", "bt_set_cell_diffusion",
+    "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
+    "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations",
+]
+
+
+class BtError(RuntimeError):
+    """A libbtgpu call returned a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (_ERRNAMES.get(code, "BT_ERR"), code, msg))
+        self.code = code
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [("n_vertices", C.c_int64), ("n_cells", C.c_int64), ("n_dofs", C.c_int64),
+                ("nnz", C.c_int64), ("n_interface_facets", C.c_int64),
+                ("n_compartments", C.c_int32), ("n_colours", C.c_int32),
+                ("sell_entries", C.c_int64), ("volume", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("max_iterations", C.c_int32),
+                ("total_iterations", C.c_int64), ("max_rel_residual", C.c_double),
+                ("gpu_ms", C.c_double), ("refinements", C.c_int32),
+                ("graph_launches", C.c_int32), ("kernel_launches", C.c_int64),
+                ("stepper_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I32 = C.POINTER(C.c_int32)
+
+
+def load(path=None):
+    """Load libbtgpu.so (once).  Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError("libbtgpu.so not found at %s: build it with __graft_entry__.build() "
+                           "(there is no CPU fallback)" % path)
+    lib = C.CDLL(path)
+    sig = {
+        "bt_version": (C.c_int, []),
+        "bt_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+        "bt_destroy": (C.c_int, [_P]),
+        "bt_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
+        "bt_set_stream": (C.c_int, [_P, _P]),
+        "bt_mesh_upload": (C.c_int, [_P, _D, C.c_int64, _I32, C.c_int64, _I32, C.c_int32, _I32]),
+        "bt_mesh_info": (C.c_int, [_P, C.POINTER(MeshInfo)]),
+        "bt_set_coefficients": (C.c_int, [_P, _D, _D, _D]),
+        "bt_set_cell_diffusion": (C.c_int, [_P, _D]),
+        "bt_assemble": (C.c_int, [_P]),
+        "bt_set_schedule": (C.c_int, [_P, _D, _D, C.c_int32, C.c_int32, C.c_double, C.c_double]),
+        "bt_solve": (C.c_int, [_P, C.c_int32, _D, _D, _I32, _D, C.c_int32, C.c_double, C.c_int32,
+                               _D, _D, _D, C.POINTER(Stats)]),
+        "bt_get_csr": (C.c_int, [_P, _I32, _I32]),
+        "bt_get_matrix": (C.c_int, [_P, C.c_int32, _D]),
+        "bt_get_dofs": (C.c_int, [_P, _I32, _I32, _D]),
+        "bt_get_colouring": (C.c_int, [_P, _I32]),
+        "bt_get_solution": (C.c_int, [_P, C.c_int32, _D]),
+        "bt_get_iterations": (C.c_int, [_P, _I32, C.c_int64]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(_I32)
+
+
+class Context:
+    """One libbtgpu context (device memory, stream, assembled matrices)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = _P()
+        rc = self.lib.bt_create(C.byref(h), int(device))
+        if rc != BT_OK:
+            raise BtError(rc, "bt_create failed (no usable CUDA device?)")
+        self.h = h
+        self.n_vertices = 0
+        self.n_regions = 0
+        self.n_compartments = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != BT_OK:
+            buf = C.create_string_buffer(1024)
+            self.lib.bt_last_error(self.h, buf, 1024)
+            raise BtError(rc, buf.value.decode(errors="replace"))
+
+    def set_stream(self, stream_ptr):
+        self._check(self.lib.bt_set_stream(self.h, _P(stream_ptr) if stream_ptr else None))
+
+    def mesh_upload(self, xyz, tets, cell_region, n_regions=None, region_compartment=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        tets = np.ascontiguousarray(tets, dtype=np.int32)
+        reg = np.ascontiguousarray(cell_region, dtype=np.int32)
+        if n_regions is None:
+            n_regions = int(reg.max()) + 1 if len(reg) else 1
+        rc_arr = None if region_compartment is None else np.ascontiguousarray(region_compartment, dtype=np.int32)
+        self._check(self.lib.bt_mesh_upload(self.h, _dp(xyz), len(xyz), _ip(tets), len(tets), _ip(reg),
+                                            int(n_regions), _ip(rc_arr)))
+        self.n_vertices = len(xyz)
+        self.n_regions = int(n_regions)
+        self.n_compartments = self.info()["n_compartments"]
+
+    def info(self):
+        mi = MeshInfo()
+        self._check(self.lib.bt_mesh_info(self.h, C.byref(mi)))
+        return {k: getattr(mi, k) for k, _ in mi._fields_}
+
+    def set_coefficients(self, D_region, invT2_region=None, kappa_pair=None):
+        D = np.ascontiguousarray(np.broadcast_to(np.asarray(D_region, np.float64), (self.n_regions,)))
+        iT2 = None if invT2_region is None else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(invT2_region, np.float64), (self.n_regions,)))
+        kp = None
+        if kappa_pair is not None:
+            kp = np.asarray(kappa_pair, np.float64)
+            if kp.ndim == 0:
+                kp = np.full((self.n_regions, self.n_regions), float(kp))
+            kp = np.ascontiguousarray(kp.reshape(self.n_regions, self.n_regions))
+        self._check(self.lib.bt_set_coefficients(self.h, _dp(D), _dp(iT2), _dp(kp)))
+
+    def set_cell_diffusion(self, D_cell6):
+        arr = None if D_cell6 is None else np.ascontiguousarray(D_cell6, dtype=np.float64)
+        self._check(self.lib.bt_set_cell_diffusion(self.h, _dp(arr)))
+
+    def assemble(self):
+        self._check(self.lib.bt_assemble(self.h))
+
+    def set_schedule(self, f_new, f_old, dt, theta=0.5):
+        fn = np.ascontiguousarray(np.atleast_2d(np.asarray(f_new, np.float64)))
+        fo = np.ascontiguousarray(np.atleast_2d(np.asarray(f_old, np.float64)))
+        if fn.shape != fo.shape:
+            raise ValueError("f_new and f_old must have the same shape")
+        self._check(self.lib.bt_set_schedule(self.h, _dp(fn), _dp(fo), fn.shape[1], fn.shape[0],
+                                             float(dt), float(theta)))
+
+    def solve(self, q, gdir, sequence=None, u0=None, precision=PRECISION_FP64, rtol=1e-12,
+              max_iterations=2000, compartments=False):
+        q = np.ascontiguousarray(np.atleast_1d(np.asarray(q, np.float64)))
+        n = len(q)
+        g = np.ascontiguousarray(np.asarray(gdir, np.float64).reshape(n, 3))
+        seq = None if sequence is None else np.ascontiguousarray(np.asarray(sequence, np.int32).reshape(n))
+        u = None if u0 is None else np.ascontiguousarray(np.asarray(u0, np.float64).reshape(self.n_vertices))
+        sig = np.zeros(n)
+        comp = np.zeros(n * self.n_compartments) if compartments else None
+        S0 = C.c_double(0.0)
+        st = Stats()
+        self._check(self.lib.bt_solve(self.h, n, _dp(q), _dp(g), _ip(seq), _dp(u), int(precision),
+                                      float(rtol), int(max_iterations), _dp(sig), _dp(comp),
+                                      C.byref(S0), C.byref(st)))
+        out = {"signal": sig, "S0": S0.value, "stats": st.as_dict()}
+        if compartments:
+            out["compartments"] = comp.reshape(n, self.n_compartments)
+        return out
+
+    def csr(self):
+        inf = self.info()
+        rp = np.zeros(inf["n_dofs"] + 1, np.int32)
+        col = np.zeros(inf["nnz"], np.int32)
+        self._check(self.lib.bt_get_csr(self.h, _ip(rp), _ip(col)))
+        return rp, col
+
+    def matrix(self, which):
+        inf = self.info()
+        v = np.zeros(inf["nnz"])
+        self._check(self.lib.bt_get_matrix(self.h, MATRICES[which], _dp(v)))
+        return v
+
+    def dofs(self):
+        inf = self.info()
+        dv = np.zeros(inf["n_dofs"], np.int32)
+        dc = np.zeros(inf["n_dofs"], np.int32)
+        w = np.zeros(inf["n_dofs"])
+        self._check(self.lib.bt_get_dofs(self.h, _ip(dv), _ip(dc), _dp(w)))
+        return dv, dc, w
+
+    def colouring(self):
+        c = np.zeros(self.info()["n_cells"], np.int32)
+        self._check(self.lib.bt_get_colouring(self.h, _ip(c)))
+        return c
+
+    def solution(self, index=0):
+        u = np.zeros(2 * self.info()["n_dofs"])
+        self._check(self.lib.bt_get_solution(self.h, int(index), _dp(u)))
+        return u[0::2] + 1j * u[1::2]
+
+    def iterations(self, n_signals, n_steps):
+        it = np.zeros(n_signals * n_steps, np.int32)
+        self._check(self.lib.bt_get_iterations(self.h, _ip(it), it.size))
+        return it.reshape(n_signals, n_steps)

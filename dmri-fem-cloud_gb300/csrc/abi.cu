@@ -1,0 +1,342 @@
+// extern "C" entry points of libbtgpu (declared in include/btgpu.h).  Every
+// function converts exceptions into a status code and records the message in
+// the context; nothing here calls exit().
+#include "bt_common.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <new>
+
+namespace bt {
+void free_solver64(bt_ctx* ctx);
+void free_solver_mixed(bt_ctx* ctx);
+}  // namespace bt
+
+namespace {
+
+template <typename F>
+int guarded(bt_ctx* ctx, F&& f) {
+    try {
+        f();
+        if (ctx) ctx->err.clear();
+        return BT_OK;
+    } catch (const bt::Error& e) {
+        if (ctx) ctx->err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        if (ctx) ctx->err = "host allocation failed";
+        return BT_ERR_OOM;
+    } catch (const std::exception& e) {
+        if (ctx) ctx->err = e.what();
+        return BT_ERR_INVALID;
+    }
+}
+
+void use_device(bt_ctx* ctx) { BT_CUDA(cudaSetDevice(ctx->device)); }
+
+}  // namespace
+
+extern "C" {
+
+int bt_version(void) { return 100; }
+
+int bt_create(bt_ctx** out, int device) {
+    if (!out) return BT_ERR_INVALID;
+    *out = nullptr;
+    bt_ctx* ctx = nullptr;
+    try {
+        ctx = new bt_ctx();
+    } catch (...) {
+        return BT_ERR_OOM;
+    }
+    ctx->device = device;
+    int rc = guarded(ctx, [&] {
+        int ndev = 0;
+        BT_CUDA(cudaGetDeviceCount(&ndev));
+        BT_REQUIRE(device >= 0 && device < ndev, BT_ERR_INVALID, "no such CUDA device");
+        use_device(ctx);
+        BT_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+        ctx->stream = ctx->own_stream;
+        BT_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+        int coop = 0;
+        BT_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+        BT_REQUIRE(coop, BT_ERR_CUDA, "device does not support cooperative launches");
+        BT_CUDA(cudaEventCreate(&ctx->ev0));
+        BT_CUDA(cudaEventCreate(&ctx->ev1));
+        BT_CUDA(cudaEventCreate(&ctx->ev2));
+    });
+    if (rc != BT_OK) {
+        bt_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return BT_OK;
+}
+
+int bt_destroy(bt_ctx* ctx) {
+    if (!ctx) return BT_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    bt::free_solver64(ctx);
+    bt::free_solver_mixed(ctx);
+    ctx->mesh = bt::Mesh();
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return BT_OK;
+}
+
+int bt_last_error(const bt_ctx* ctx, char* buf, size_t len) {
+    if (!ctx || !buf || len == 0) return BT_ERR_INVALID;
+    std::strncpy(buf, ctx->err.c_str(), len - 1);
+    buf[len - 1] = '\0';
+    return BT_OK;
+}
+
+int bt_set_stream(bt_ctx* ctx, void* cuda_stream) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        use_device(ctx);
+        BT_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    });
+}
+
+int bt_mesh_upload(bt_ctx* ctx, const double* xyz, int64_t n_vertices, const int32_t* tets, int64_t n_cells,
+                   const int32_t* cell_region, int32_t n_regions, const int32_t* region_compartment) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(xyz && tets && cell_region, BT_ERR_INVALID, "bt_mesh_upload: NULL array");
+        use_device(ctx);
+        ctx->mat.done = false;
+        ctx->coeffs = bt::Coeffs();
+        bt::free_solver64(ctx);
+        bt::free_solver_mixed(ctx);
+        bt::build_graph(ctx, xyz, n_vertices, tets, n_cells, cell_region, n_regions, region_compartment);
+    });
+}
+
+int bt_mesh_info(bt_ctx* ctx, bt_mesh_info_t* out) {
+    if (!ctx || !out) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Mesh& m = ctx->mesh;
+        BT_REQUIRE(m.built, BT_ERR_STATE, "bt_mesh_info: no mesh");
+        out->n_vertices = m.n_v;
+        out->n_cells = m.n_t;
+        out->n_dofs = m.n_dofs;
+        out->nnz = m.nnz;
+        out->n_interface_facets = m.n_iface;
+        out->n_compartments = m.n_comp;
+        out->n_colours = m.n_colours;
+        out->sell_entries = m.sell_entries;
+        out->volume = m.volume;
+    });
+}
+
+int bt_set_coefficients(bt_ctx* ctx, const double* D_region, const double* invT2_region,
+                        const double* kappa_pair) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Mesh& m = ctx->mesh;
+        BT_REQUIRE(m.built, BT_ERR_STATE, "bt_set_coefficients: no mesh");
+        BT_REQUIRE(D_region, BT_ERR_INVALID, "bt_set_coefficients: D_region is NULL");
+        use_device(ctx);
+        const int nr = m.n_regions;
+        std::vector<double> D(D_region, D_region + nr), iT2(nr, 0.0), kp((size_t)nr * nr, 0.0);
+        for (int r = 0; r < nr; ++r) BT_REQUIRE(std::isfinite(D[r]) && D[r] >= 0.0, BT_ERR_INVALID, "D must be finite and >= 0");
+        if (invT2_region)
+            for (int r = 0; r < nr; ++r) {
+                iT2[r] = invT2_region[r];
+                BT_REQUIRE(std::isfinite(iT2[r]) && iT2[r] >= 0.0, BT_ERR_INVALID, "1/T2 must be finite and >= 0");
+            }
+        if (kappa_pair)
+            for (int i = 0; i < nr * nr; ++i) {
+                kp[i] = kappa_pair[i];
+                BT_REQUIRE(std::isfinite(kp[i]) && kp[i] >= 0.0, BT_ERR_INVALID, "kappa must be finite and >= 0");
+            }
+        for (int i = 0; i < nr; ++i)
+            for (int j = 0; j < nr; ++j)
+                BT_REQUIRE(kp[(size_t)i * nr + j] == kp[(size_t)j * nr + i], BT_ERR_INVALID, "kappa_pair must be symmetric");
+        bt::Coeffs& c = ctx->coeffs;
+        c.D_region.upload(D.data(), nr, ctx->stream);
+        c.invT2_region.upload(iT2.data(), nr, ctx->stream);
+        c.kappa_pair.upload(kp.data(), (size_t)nr * nr, ctx->stream);
+        BT_CUDA(cudaStreamSynchronize(ctx->stream));
+        c.set = true;
+        ctx->mat.done = false;
+    });
+}
+
+int bt_set_cell_diffusion(bt_ctx* ctx, const double* D_cell) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Mesh& m = ctx->mesh;
+        BT_REQUIRE(m.built, BT_ERR_STATE, "bt_set_cell_diffusion: no mesh");
+        use_device(ctx);
+        bt::Coeffs& c = ctx->coeffs;
+        if (!D_cell) {
+            c.D_cell.release();
+            c.has_cell_D = false;
+        } else {
+            for (int64_t i = 0; i < m.n_t * 6; ++i)
+                BT_REQUIRE(std::isfinite(D_cell[i]), BT_ERR_INVALID, "D_cell must be finite");
+            c.D_cell.upload(D_cell, (size_t)m.n_t * 6, ctx->stream);
+            BT_CUDA(cudaStreamSynchronize(ctx->stream));
+            c.has_cell_D = true;
+        }
+        ctx->mat.done = false;
+    });
+}
+
+int bt_assemble(bt_ctx* ctx) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        use_device(ctx);
+        bt::assemble_all(ctx);
+    });
+}
+
+int bt_set_schedule(bt_ctx* ctx, const double* f_new, const double* f_old, int32_t n_steps, int32_t n_sequences,
+                    double dt, double theta) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(f_new && f_old, BT_ERR_INVALID, "bt_set_schedule: NULL schedule");
+        BT_REQUIRE(n_steps >= 1 && n_sequences >= 1, BT_ERR_INVALID, "bt_set_schedule: empty schedule");
+        BT_REQUIRE(std::isfinite(dt) && dt > 0.0, BT_ERR_INVALID, "dt must be > 0");
+        BT_REQUIRE(std::isfinite(theta) && theta > 0.0 && theta <= 1.0, BT_ERR_INVALID, "theta must be in (0, 1]");
+        const size_t n = (size_t)n_steps * n_sequences;
+        for (size_t i = 0; i < n; ++i)
+            BT_REQUIRE(std::isfinite(f_new[i]) && std::isfinite(f_old[i]), BT_ERR_INVALID, "schedule must be finite");
+        bt::Schedule& S = ctx->sched;
+        S.f_new.assign(f_new, f_new + n);
+        S.f_old.assign(f_old, f_old + n);
+        S.n_steps = n_steps;
+        S.n_seq = n_sequences;
+        S.dt = dt;
+        S.theta = theta;
+        S.set = true;
+    });
+}
+
+int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir, const int32_t* sequence,
+             const double* u0, int32_t precision, double rtol, int32_t max_iterations, double* signal_out,
+             double* compartment_out, double* S0_out, bt_stats* stats) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_solve: mesh not assembled");
+        BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_solve: no schedule");
+        BT_REQUIRE(n_signals >= 1 && q && gdir && signal_out, BT_ERR_INVALID, "bt_solve: bad arguments");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_solve: rtol must be > 0 and max_iterations >= 1");
+        for (int32_t i = 0; i < n_signals; ++i) {
+            BT_REQUIRE(std::isfinite(q[i]), BT_ERR_INVALID, "bt_solve: q must be finite");
+            const double g0 = gdir[3 * i], g1 = gdir[3 * i + 1], g2 = gdir[3 * i + 2];
+            BT_REQUIRE(std::isfinite(g0) && std::isfinite(g1) && std::isfinite(g2), BT_ERR_INVALID,
+                       "bt_solve: gradient direction must be finite");
+        }
+        if (u0)
+            for (int64_t v = 0; v < ctx->mesh.n_v; ++v)
+                BT_REQUIRE(std::isfinite(u0[v]), BT_ERR_INVALID, "bt_solve: u0 must be finite");
+        use_device(ctx);
+        ctx->last_precision = -1;
+        if (precision == BT_PRECISION_FP64) {
+            bt::solve_fp64(ctx, n_signals, q, gdir, sequence, u0, rtol, max_iterations, signal_out,
+                           compartment_out, stats);
+        } else if (precision == BT_PRECISION_MIXED) {
+            bt::solve_mixed(ctx, n_signals, q, gdir, sequence, u0, rtol, max_iterations, signal_out,
+                            compartment_out, stats);
+        } else {
+            throw bt::Error(BT_ERR_INVALID, "bt_solve: unknown precision");
+        }
+        ctx->last_precision = precision;
+        if (S0_out) {
+            if (u0) {
+                bt::DevBuf<double> d;
+                d.upload(u0, ctx->mesh.n_v, ctx->stream);
+                *S0_out = bt::device_dot(ctx->mat.vw, d, ctx->mesh.n_v, ctx->stream);
+            } else {
+                *S0_out = ctx->mesh.volume;
+            }
+        }
+    });
+}
+
+int bt_get_csr(bt_ctx* ctx, int32_t* row_ptr, int32_t* col) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Mesh& m = ctx->mesh;
+        BT_REQUIRE(m.built, BT_ERR_STATE, "bt_get_csr: no mesh");
+        use_device(ctx);
+        if (row_ptr) m.row_ptr.download(row_ptr, m.n_dofs + 1, ctx->stream);
+        if (col) m.col.download(col, m.nnz, ctx->stream);
+        BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int bt_get_matrix(bt_ctx* ctx, int32_t which, double* values) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mat.done, BT_ERR_STATE, "bt_get_matrix: not assembled");
+        BT_REQUIRE(values, BT_ERR_INVALID, "bt_get_matrix: NULL output");
+        use_device(ctx);
+        const bt::DevBuf<double>* src[] = {&ctx->mat.M, &ctx->mat.K, &ctx->mat.T, &ctx->mat.R,
+                                           &ctx->mat.Jx, &ctx->mat.Jy, &ctx->mat.Jz};
+        BT_REQUIRE(which >= 0 && which < 7, BT_ERR_INVALID, "bt_get_matrix: unknown matrix");
+        src[which]->download(values, ctx->mesh.nnz, ctx->stream);
+        BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int bt_get_dofs(bt_ctx* ctx, int32_t* dof_vertex, int32_t* dof_compartment, double* weights) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Mesh& m = ctx->mesh;
+        BT_REQUIRE(m.built, BT_ERR_STATE, "bt_get_dofs: no mesh");
+        use_device(ctx);
+        if (dof_vertex) m.dof_vertex.download(dof_vertex, m.n_dofs, ctx->stream);
+        if (dof_compartment) m.dof_comp.download(dof_compartment, m.n_dofs, ctx->stream);
+        if (weights) {
+            BT_REQUIRE(ctx->mat.done, BT_ERR_STATE, "bt_get_dofs: weights need bt_assemble");
+            ctx->mat.w.download(weights, m.n_dofs, ctx->stream);
+        }
+        BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int bt_get_colouring(bt_ctx* ctx, int32_t* cell_colour) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Mesh& m = ctx->mesh;
+        BT_REQUIRE(m.built && cell_colour, BT_ERR_INVALID, "bt_get_colouring: no mesh or NULL output");
+        use_device(ctx);
+        m.colour.download(cell_colour, m.n_t, ctx->stream);
+        BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int bt_get_solution(bt_ctx* ctx, int32_t index, double* u) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(u, BT_ERR_INVALID, "bt_get_solution: NULL output");
+        use_device(ctx);
+        BT_REQUIRE(ctx->last_precision >= 0, BT_ERR_STATE, "bt_get_solution: no solve yet");
+        if (ctx->last_precision == BT_PRECISION_MIXED)
+            bt::get_solution_mixed(ctx, index, u);
+        else
+            bt::get_solution_fp64(ctx, index, u);
+    });
+}
+
+int bt_get_iterations(bt_ctx* ctx, int32_t* iters, int64_t capacity) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(iters, BT_ERR_INVALID, "bt_get_iterations: NULL output");
+        BT_REQUIRE(capacity >= (int64_t)ctx->last_iters.size(), BT_ERR_INVALID,
+                   "bt_get_iterations: buffer smaller than n_signals*n_steps");
+        std::memcpy(iters, ctx->last_iters.data(), ctx->last_iters.size() * sizeof(int32_t));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,478 @@
+// FP64 Crank-Nicolson / Jacobi-COCG time stepper: one persistent cooperative
+// kernel integrates a whole signal.
+//
+// Reference: MRI_simulation.solve (DmriFemLib.py:878-915).  Each step of the
+// reference assembles A = M/k + F(f(t)) and b = L(u, f(tp)) and calls a PETSc
+// Krylov solver (DmriFemLib.py:901-907).  In complex form (u = ur + i ui,
+// duplicated interface dofs) the step is
+//     (A_re + i cn J_g) u_new = (B_re - i co J_g) u_old
+//     A_re = M/k + theta (K + T + R),  B_re = M/k - (1 - theta)(K + T + R),
+//     cn = theta q f(t),  co = (1 - theta) q f(tp),
+// complex symmetric, so it is solved with COCG (CG with the unconjugated
+// bilinear form) and the Jacobi preconditioner diag(A)^-1.
+//
+// Layout: the matrix lives in sliced ELL (32 rows per slice, column-major in a
+// slice) packed per signal as double2 {A_re, J_g} plus B_re, so a warp reads
+// 32 consecutive 16-byte entries per column step (coalesced 128-bit loads).
+// Vectors are double2 (re, im) of length n_pad = 32 * slices.
+//
+// One kernel runs all steps and iterations; phases are separated by a bounded
+// grid barrier (bt_common.cuh).  Two barriers per COCG iteration: the search
+// direction update p = z + beta p is folded into the SpMV (each row forms
+// z_j + beta p_j of its neighbours on the fly and the owner writes its own p
+// to a second buffer), so the iteration is
+//   phase A:  p' = z + beta p,  q = A p',  mu = p'^T q           | barrier
+//   phase B:  x += alpha p', r -= alpha q, z = D^-1 r, rho = r^T z | barrier
+// Reductions are per-block partials summed by every block in block order, so
+// all blocks take identical decisions and results are bitwise reproducible.
+#include "bt_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace bt {
+
+constexpr int kThreads64 = 256;
+constexpr int kRed = 1 + kMaxCompartments;  // reduction width of the signal phase
+
+struct Solver64 {
+    int64_t n_pad = 0, sell = 0;
+    int32_t nblocks = 0;
+    DevBuf<double2> aj;          // SELL {A_re, J_g}
+    DevBuf<double> bre;          // SELL B_re
+    DevBuf<double> dA, dJ, w;    // per row
+    DevBuf<int32_t> rcomp;       // compartment per row (-1 padding)
+    DevBuf<double2> x, r, z, pa, pb, q;
+    DevBuf<double> partials;
+    DevBuf<unsigned> bar;
+    DevBuf<int> status;
+    DevBuf<double> cn, co, relres, out;
+    DevBuf<int32_t> iters;
+    DevBuf<double> gq;           // gradient direction for the pack kernel
+    DevBuf<double2> saved;       // final solutions [nsig][n_pad]
+    int32_t saved_nsig = 0;
+};
+
+struct StepArgs {
+    int32_t n_slices;
+    const int32_t* __restrict__ sl_ptr;
+    const int32_t* __restrict__ sl_w;
+    const int32_t* __restrict__ col;
+    const double2* __restrict__ aj;
+    const double* __restrict__ bre;
+    const double* __restrict__ dA;
+    const double* __restrict__ dJ;
+    const double* __restrict__ w;
+    const int32_t* __restrict__ rcomp;
+    double2* x;
+    double2* r;
+    double2* z;
+    double2* pa;
+    double2* pb;
+    double2* q;
+    double* partials;
+    unsigned* bar;
+    int* status;
+    const double* __restrict__ cn;
+    const double* __restrict__ co;
+    int32_t n_steps;
+    int32_t maxit;
+    int32_t nc;
+    double rtol2;
+    int32_t* iters;
+    double* relres;
+    double* out;
+};
+
+// Grid-wide deterministic sum of NV doubles: block partials go to one of two
+// alternating buffers (a block may start the next reduction while a slower
+// block is still reading the previous one), then every block adds the
+// partials in block order.  On return every thread holds the sums in v[].
+template <int NV>
+__device__ __forceinline__ bool reduce_all(double (&v)[NV], double* partials, unsigned nb, unsigned& flip,
+                                           unsigned* bar, int* status, unsigned& gen, double* sm,
+                                           double* red) {
+    block_sum<NV>(v, sm);
+    double* P = partials + (size_t)(flip & 1u) * nb * kRed;
+    ++flip;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) P[blockIdx.x * kRed + k] = v[k];
+    }
+    if (!grid_barrier(bar, nb, status, gen)) return false;
+    if ((threadIdx.x >> 5) == 0) {
+        const int lane = threadIdx.x & 31;
+        double t[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) t[k] = 0.0;
+        for (unsigned b = lane; b < nb; b += 32) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) t[k] += __ldcg(&P[b * kRed + k]);
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) t[k] = warp_sum(t[k]);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) red[k] = t[k];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = red[k];
+    __syncthreads();
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
+    __shared__ double sm[32 * kRed];
+    __shared__ double red[kRed];
+    const int lane = threadIdx.x & 31;
+    const int warps_per_block = kThreads64 / 32;
+    const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+    const int total_warps = gridDim.x * warps_per_block;
+    const unsigned nb = gridDim.x;
+    unsigned gen = 0, flip = 0;
+
+    for (int step = 0; step < a.n_steps; ++step) {
+        const double cn = a.cn[step], co = a.co[step];
+        // ---- phase R: b = (B_re - i co J) x ; r = b - (A_re + i cn J) x ; z = D^-1 r
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};  // rho.re, rho.im, |r|^2, |b|^2
+        for (int s = gw; s < a.n_slices; s += total_warps) {
+            const int32_t base = a.sl_ptr[s], wdt = a.sl_w[s];
+            double2 sA = make_double2(0.0, 0.0), sJ = sA, sB = sA;
+            for (int k = 0; k < wdt; ++k) {
+                const int32_t e = base + k * 32 + lane;
+                const int32_t c = a.col[e];
+                const double2 m = a.aj[e];
+                const double br = a.bre[e];
+                const double2 xj = a.x[c];
+                sA.x = fma(m.x, xj.x, sA.x); sA.y = fma(m.x, xj.y, sA.y);
+                sJ.x = fma(m.y, xj.x, sJ.x); sJ.y = fma(m.y, xj.y, sJ.y);
+                sB.x = fma(br, xj.x, sB.x);  sB.y = fma(br, xj.y, sB.y);
+            }
+            const int64_t i = (int64_t)s * 32 + lane;
+            const double2 b = make_double2(fma(co, sJ.y, sB.x), fma(-co, sJ.x, sB.y));
+            const double2 ax = make_double2(fma(-cn, sJ.y, sA.x), fma(cn, sJ.x, sA.y));
+            const double2 rr = make_double2(b.x - ax.x, b.y - ax.y);
+            const double2 zz = cmul(cinv(make_double2(a.dA[i], cn * a.dJ[i])), rr);
+            a.r[i] = rr;
+            a.z[i] = zz;
+            const double2 rz = cmul(rr, zz);
+            acc[0] += rz.x;
+            acc[1] += rz.y;
+            acc[2] += rr.x * rr.x + rr.y * rr.y;
+            acc[3] += b.x * b.x + b.y * b.y;
+        }
+        if (!reduce_all<4>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+        double2 rho = make_double2(acc[0], acc[1]);
+        double rr2 = acc[2];
+        const double bb2 = acc[3];
+        const double tol2 = a.rtol2 * bb2;
+        double2 beta = make_double2(0.0, 0.0);
+        double2* pold = a.pa;
+        double2* pnew = a.pb;
+        int it = 0;
+        bool failed = false;  // uniform across the grid: every block sees the same sums
+        while (rr2 > tol2) {
+            if (it >= a.maxit) {
+                if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
+                failed = true;
+                break;
+            }
+            // ---- phase A: p' = z + beta p ; q = A p' ; mu = p'^T q
+            double mu[2] = {0.0, 0.0};
+            for (int s = gw; s < a.n_slices; s += total_warps) {
+                const int32_t base = a.sl_ptr[s], wdt = a.sl_w[s];
+                double2 sA = make_double2(0.0, 0.0), sJ = sA;
+                for (int k = 0; k < wdt; ++k) {
+                    const int32_t e = base + k * 32 + lane;
+                    const int32_t c = a.col[e];
+                    const double2 m = a.aj[e];
+                    const double2 zc = a.z[c], pc = pold[c];
+                    const double2 pj = make_double2(zc.x + (beta.x * pc.x - beta.y * pc.y),
+                                                    zc.y + (beta.x * pc.y + beta.y * pc.x));
+                    sA.x = fma(m.x, pj.x, sA.x); sA.y = fma(m.x, pj.y, sA.y);
+                    sJ.x = fma(m.y, pj.x, sJ.x); sJ.y = fma(m.y, pj.y, sJ.y);
+                }
+                const int64_t i = (int64_t)s * 32 + lane;
+                const double2 zi = a.z[i], pi = pold[i];
+                const double2 pn = make_double2(zi.x + (beta.x * pi.x - beta.y * pi.y),
+                                                zi.y + (beta.x * pi.y + beta.y * pi.x));
+                const double2 qi = make_double2(fma(-cn, sJ.y, sA.x), fma(cn, sJ.x, sA.y));
+                pnew[i] = pn;
+                a.q[i] = qi;
+                const double2 pq = cmul(pn, qi);
+                mu[0] += pq.x;
+                mu[1] += pq.y;
+            }
+            if (!reduce_all<2>(mu, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+            const double2 muv = make_double2(mu[0], mu[1]);
+            const double mun = muv.x * muv.x + muv.y * muv.y;
+            if (!(mun > 0.0) || !isfinite(mun)) {
+                if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_BREAKDOWN);
+                failed = true;
+                break;
+            }
+            const double2 alpha = cdiv(rho, muv);
+            // ---- phase B: x += alpha p' ; r -= alpha q ; z = D^-1 r
+            double acc3[3] = {0.0, 0.0, 0.0};
+            for (int s = gw; s < a.n_slices; s += total_warps) {
+                const int64_t i = (int64_t)s * 32 + lane;
+                const double2 pn = pnew[i], qi = a.q[i];
+                double2 xi = a.x[i], ri = a.r[i];
+                const double2 ap = cmul(alpha, pn), aq = cmul(alpha, qi);
+                xi.x += ap.x; xi.y += ap.y;
+                ri.x -= aq.x; ri.y -= aq.y;
+                const double2 zi = cmul(cinv(make_double2(a.dA[i], cn * a.dJ[i])), ri);
+                a.x[i] = xi;
+                a.r[i] = ri;
+                a.z[i] = zi;
+                const double2 rz = cmul(ri, zi);
+                acc3[0] += rz.x;
+                acc3[1] += rz.y;
+                acc3[2] += ri.x * ri.x + ri.y * ri.y;
+            }
+            if (!reduce_all<3>(acc3, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+            const double2 rho_new = make_double2(acc3[0], acc3[1]);
+            rr2 = acc3[2];
+            ++it;
+            const double rhon = rho.x * rho.x + rho.y * rho.y;
+            if (!(rhon > 0.0) || !isfinite(rr2)) {
+                if (rr2 > tol2 || !isfinite(rr2)) {
+                    if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_BREAKDOWN);
+                    failed = true;
+                }
+                break;
+            }
+            beta = cdiv(rho_new, rho);
+            rho = rho_new;
+            double2* t = pold;
+            pold = pnew;
+            pnew = t;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.iters[step] = it;
+            a.relres[step] = (bb2 > 0.0) ? sqrt(rr2 / bb2) : sqrt(rr2);
+        }
+        if (failed) return;
+        // The last phase B (or phase R when no iteration ran) ended in a grid
+        // barrier, so every x written this step is visible to the next phase R.
+    }
+    // ---- signal: S = sum w Re(x), per compartment
+    double acc[kRed];
+#pragma unroll
+    for (int k = 0; k < kRed; ++k) acc[k] = 0.0;
+    for (int s = gw; s < a.n_slices; s += total_warps) {
+        const int64_t i = (int64_t)s * 32 + lane;
+        const int c = a.rcomp[i];
+        if (c >= 0) {
+            const double v = a.w[i] * a.x[i].x;
+            acc[0] += v;
+#pragma unroll
+            for (int k = 0; k < kMaxCompartments; ++k)
+                if (k == c) acc[1 + k] += v;
+        }
+    }
+    if (!reduce_all<kRed>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+    if (blockIdx.x == 0 && threadIdx.x < kRed) a.out[threadIdx.x] = red[threadIdx.x];
+}
+
+// Pack the SELL values of one signal: {A_re, J_g}, B_re, and the diagonals.
+__global__ void k_pack64(int64_t sell, const int32_t* __restrict__ sl_pos, const double* __restrict__ M,
+                         const double* __restrict__ K, const double* __restrict__ T, const double* __restrict__ R,
+                         const double* __restrict__ Jx, const double* __restrict__ Jy,
+                         const double* __restrict__ Jz, const double* __restrict__ g, double inv_k,
+                         double theta, double2* __restrict__ aj, double* __restrict__ bre) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= sell) return;
+    const int32_t p = sl_pos[e];
+    if (p < 0) {
+        aj[e] = make_double2(0.0, 0.0);
+        bre[e] = 0.0;
+        return;
+    }
+    const double mk = M[p] * inv_k;
+    const double S = K[p] + T[p] + R[p];
+    aj[e] = make_double2(mk + theta * S, g[0] * Jx[p] + g[1] * Jy[p] + g[2] * Jz[p]);
+    bre[e] = mk - (1.0 - theta) * S;
+}
+
+__global__ void k_rows64(int64_t n, int64_t n_pad, const int32_t* __restrict__ diag_pos,
+                         const double* __restrict__ M, const double* __restrict__ K, const double* __restrict__ T,
+                         const double* __restrict__ R, const double* __restrict__ Jx,
+                         const double* __restrict__ Jy, const double* __restrict__ Jz,
+                         const double* __restrict__ g, double inv_k, double theta,
+                         const double* __restrict__ wsrc, const int32_t* __restrict__ comp,
+                         const int32_t* __restrict__ dof_vertex, const double* __restrict__ u0,
+                         double* __restrict__ dA, double* __restrict__ dJ, double* __restrict__ w,
+                         int32_t* __restrict__ rcomp, double2* __restrict__ x, double2* __restrict__ pa,
+                         double2* __restrict__ pb) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    if (i < n) {
+        const int32_t p = diag_pos[i];
+        dA[i] = M[p] * inv_k + theta * (K[p] + T[p] + R[p]);
+        dJ[i] = g[0] * Jx[p] + g[1] * Jy[p] + g[2] * Jz[p];
+        w[i] = wsrc[i];
+        rcomp[i] = comp[i];
+        x[i] = make_double2(u0 ? u0[dof_vertex[i]] : 1.0, 0.0);
+    } else {
+        dA[i] = 1.0;
+        dJ[i] = 0.0;
+        w[i] = 0.0;
+        rcomp[i] = -1;
+        x[i] = make_double2(0.0, 0.0);
+    }
+    pa[i] = make_double2(0.0, 0.0);
+    pb[i] = make_double2(0.0, 0.0);
+}
+
+static void map_status(int st) {
+    switch (st) {
+        case DEV_OK: return;
+        case DEV_TIMEOUT: throw Error(BT_ERR_TIMEOUT, "stepper: a grid barrier wait ran out of time");
+        case DEV_NOT_CONVERGED: throw Error(BT_ERR_NOT_CONVERGED, "stepper: COCG reached max_iterations");
+        case DEV_BREAKDOWN: throw Error(BT_ERR_BREAKDOWN, "stepper: COCG breakdown (p^T A p = 0)");
+        default: throw Error(BT_ERR_CUDA, "stepper: device status " + std::to_string(st));
+    }
+}
+
+void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
+                const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st) {
+    Mesh& m = ctx->mesh;
+    Assembled& A = ctx->mat;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    if (!ctx->s64) ctx->s64 = new Solver64();
+    Solver64& W = *ctx->s64;
+    const int64_t n = m.n_dofs;
+    W.n_pad = (int64_t)m.n_slices * 32;
+    W.sell = m.sell_entries;
+    W.aj.alloc(W.sell);
+    W.bre.alloc(W.sell);
+    W.dA.alloc(W.n_pad); W.dJ.alloc(W.n_pad); W.w.alloc(W.n_pad);
+    W.rcomp.alloc(W.n_pad);
+    for (auto* v : {&W.x, &W.r, &W.z, &W.pa, &W.pb, &W.q}) v->alloc(W.n_pad);
+    W.bar.alloc(2);
+    W.status.alloc(1);
+    W.cn.alloc(S.n_steps); W.co.alloc(S.n_steps);
+    W.relres.alloc(S.n_steps);
+    W.iters.alloc(S.n_steps);
+    W.out.alloc(kRed);
+    W.gq.alloc(3);
+    W.saved.alloc((size_t)nsig * W.n_pad);
+    W.saved_nsig = nsig;
+    DevBuf<double> d_u0;
+    if (u0) d_u0.upload(u0, m.n_v, s);
+
+    // grid: co-resident blocks, no more than the slices need
+    int per_sm = 0;
+    BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step64, kThreads64, 0));
+    BT_REQUIRE(per_sm >= 1, BT_ERR_CUDA, "stepper kernel does not fit on an SM");
+    const int need = (m.n_slices + kThreads64 / 32 - 1) / (kThreads64 / 32);
+    W.nblocks = std::max(1, std::min(per_sm * ctx->num_sms, need));
+    W.partials.alloc((size_t)2 * W.nblocks * kRed);
+
+    const double inv_k = 1.0 / S.dt;
+    std::vector<double> hcn(S.n_steps), hco(S.n_steps), hout(kRed), hres(S.n_steps);
+    std::vector<int32_t> hit(S.n_steps);
+    ctx->last_iters.assign((size_t)nsig * S.n_steps, 0);
+    if (st) {
+        st->steps = S.n_steps;
+        st->max_iterations = 0;
+        st->total_iterations = 0;
+        st->max_rel_residual = 0.0;
+        st->refinements = 0;
+        st->graph_launches = 0;
+        st->kernel_launches = 0;
+        st->stepper_ms = 0.0;
+    }
+    float stepper_ms_total = 0.0f;
+    BT_CUDA(cudaEventRecord(ctx->ev0, s));
+    for (int32_t sg = 0; sg < nsig; ++sg) {
+        const int32_t row = seq ? seq[sg] : 0;
+        BT_REQUIRE(row >= 0 && row < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
+        const double* fn = S.f_new.data() + (size_t)row * S.n_steps;
+        const double* fo = S.f_old.data() + (size_t)row * S.n_steps;
+        for (int k = 0; k < S.n_steps; ++k) {
+            hcn[k] = S.theta * q[sg] * fn[k];
+            hco[k] = (1.0 - S.theta) * q[sg] * fo[k];
+        }
+        W.cn.upload(hcn.data(), S.n_steps, s);
+        W.co.upload(hco.data(), S.n_steps, s);
+        W.gq.upload(gdir + 3 * sg, 3, s);
+        k_pack64<<<(unsigned)((W.sell + 255) / 256), 256, 0, s>>>(W.sell, m.sl_pos, A.M, A.K, A.T, A.R, A.Jx,
+                                                                 A.Jy, A.Jz, W.gq, inv_k, S.theta, W.aj, W.bre);
+        k_rows64<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(
+            n, W.n_pad, m.diag_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz, W.gq, inv_k, S.theta, A.w, m.dof_comp,
+            m.dof_vertex, u0 ? d_u0.p : nullptr, W.dA, W.dJ, W.w, W.rcomp, W.x, W.pa, W.pb);
+        BT_CUDA(cudaGetLastError());
+        W.bar.zero(s);
+        W.status.zero(s);
+        StepArgs a;
+        a.n_slices = m.n_slices;
+        a.sl_ptr = m.sl_ptr; a.sl_w = m.sl_w; a.col = m.sl_col;
+        a.aj = W.aj; a.bre = W.bre; a.dA = W.dA; a.dJ = W.dJ; a.w = W.w; a.rcomp = W.rcomp;
+        a.x = W.x; a.r = W.r; a.z = W.z; a.pa = W.pa; a.pb = W.pb; a.q = W.q;
+        a.partials = W.partials; a.bar = W.bar; a.status = W.status;
+        a.cn = W.cn; a.co = W.co;
+        a.n_steps = S.n_steps;
+        a.maxit = maxit;
+        a.nc = m.n_comp;
+        a.rtol2 = rtol * rtol;
+        a.iters = W.iters; a.relres = W.relres; a.out = W.out;
+        void* args[] = {&a};
+        BT_CUDA(cudaEventRecord(ctx->ev1, s));
+        BT_CUDA(cudaLaunchCooperativeKernel((const void*)k_step64, dim3(W.nblocks), dim3(kThreads64), args, 0, s));
+        BT_CUDA(cudaEventRecord(ctx->ev2, s));
+        BT_CUDA(cudaMemcpyAsync(W.saved.p + (size_t)sg * W.n_pad, W.x.p, W.n_pad * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, s));
+        int hst = 0;
+        BT_CUDA(cudaMemcpyAsync(&hst, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        W.out.download(hout.data(), kRed, s);
+        W.iters.download(hit.data(), S.n_steps, s);
+        W.relres.download(hres.data(), S.n_steps, s);
+        BT_CUDA(cudaStreamSynchronize(s));
+        float ms = 0.0f;
+        BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
+        stepper_ms_total += ms;
+        map_status(hst);
+        sig[sg] = hout[0];
+        if (comp_sig)
+            for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)sg * m.n_comp + c] = hout[1 + c];
+        for (int k = 0; k < S.n_steps; ++k) {
+            ctx->last_iters[(size_t)sg * S.n_steps + k] = hit[k];
+            if (st) {
+                st->max_iterations = std::max(st->max_iterations, hit[k]);
+                st->total_iterations += hit[k];
+                st->max_rel_residual = std::max(st->max_rel_residual, hres[k]);
+            }
+        }
+        if (st) st->kernel_launches += 3;
+    }
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    BT_CUDA(cudaEventSynchronize(ctx->ev2));
+    float total_ms = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&total_ms, ctx->ev0, ctx->ev2));
+    if (st) {
+        st->gpu_ms = total_ms;
+        st->stepper_ms = stepper_ms_total;
+    }
+    ctx->last_nsig = nsig;
+}
+
+void get_solution_fp64(bt_ctx* ctx, int32_t index, double* u) {
+    BT_REQUIRE(ctx->s64 && index >= 0 && index < ctx->s64->saved_nsig, BT_ERR_INVALID,
+               "bt_get_solution: no such signal in the last FP64 solve");
+    Solver64& W = *ctx->s64;
+    BT_CUDA(cudaMemcpyAsync(u, W.saved.p + (size_t)index * W.n_pad, ctx->mesh.n_dofs * sizeof(double2),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    BT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void free_solver64(bt_ctx* ctx) {
+    delete ctx->s64;
+    ctx->s64 = nullptr;
+}
+
+}  // namespace bt

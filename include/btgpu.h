@@ -1,0 +1,168 @@
+/*
+ * btgpu.h -- C ABI of the GB300 Bloch-Torrey finite-element engine (libbtgpu.so).
+ *
+ * The library replaces the arithmetic under the reference's solver call
+ * (van-dang/DMRI-FEM-Cloud, DmriFemLib.py `MRI_simulation.solve`, lines
+ * 878-915): the per-step DOLFIN `assemble(F)`/`assemble(L)` of the theta-method
+ * forms (DmriFemLib.py:58-145, 904-905), the PETSc Krylov solve
+ * (DmriFemLib.py:907; GCloudDmriSolver.py:219-222) and the signal functional of
+ * `PostProcessing` (DmriFemLib.py:917-931).
+ *
+ * Conventions
+ *  - Every function returns an int status: BT_OK (0) or one of BT_ERR_*.
+ *    Nothing calls exit(); the text of the last failure is available from
+ *    bt_last_error().
+ *  - Host arrays are caller-owned and copied during the call.  Device memory,
+ *    the stream, events and CUDA graphs belong to the context.
+ *  - A context is not thread-safe: use one context per host thread.
+ *  - Units follow the reference: lengths in um, times in us, D in um^2/us
+ *    (numerically mm^2/s), kappa in um/us (numerically m/s), q = sqrt(b/int4gb).
+ */
+#ifndef BTGPU_H
+#define BTGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BT_OK 0
+#define BT_ERR_INVALID 1        /* bad argument or mesh                      */
+#define BT_ERR_CUDA 2           /* CUDA runtime error                        */
+#define BT_ERR_OOM 3            /* device allocation failed                  */
+#define BT_ERR_NOT_CONVERGED 4  /* a step hit max_iterations                 */
+#define BT_ERR_BREAKDOWN 5      /* COCG breakdown (p^T A p = 0)              */
+#define BT_ERR_TIMEOUT 6        /* a device-side wait ran out of time        */
+#define BT_ERR_STATE 7          /* call out of order (e.g. solve before assemble) */
+
+#define BT_PRECISION_FP64 0     /* FP64 matrices and Krylov vectors          */
+#define BT_PRECISION_MIXED 1    /* FP32 inner COCG, FP64 residual/refinement/signal */
+
+/* Matrices that bt_get_matrix() can export (values in CSR order). */
+#define BT_MAT_M 0   /* int phi_i phi_j over the dof's compartment            */
+#define BT_MAT_K 1   /* int D grad phi_i . grad phi_j                           */
+#define BT_MAT_T 2   /* int (1/T2) phi_i phi_j                                  */
+#define BT_MAT_R 3   /* kappa int_Gamma [phi_i][phi_j] on compartment interfaces */
+#define BT_MAT_JX 4  /* int x phi_i phi_j                                       */
+#define BT_MAT_JY 5  /* int y phi_i phi_j                                       */
+#define BT_MAT_JZ 6  /* int z phi_i phi_j                                       */
+
+typedef struct bt_ctx bt_ctx;
+
+typedef struct bt_mesh_info_t {
+    int64_t n_vertices;
+    int64_t n_cells;
+    int64_t n_dofs;              /* live (vertex, compartment) pairs            */
+    int64_t nnz;                 /* CSR entries of the duplicated-node graph    */
+    int64_t n_interface_facets;  /* facets between cells of different compartments */
+    int32_t n_compartments;
+    int32_t n_colours;           /* cell colours of the assembly               */
+    int64_t sell_entries;        /* sliced-ELL slots (incl. padding)            */
+    double volume;               /* sum of cell volumes                         */
+} bt_mesh_info_t;
+
+typedef struct bt_stats_t {
+    int32_t steps;               /* time steps per signal                       */
+    int32_t max_iterations;      /* largest inner iteration count of any step   */
+    int64_t total_iterations;    /* inner iterations summed over steps/signals  */
+    double max_rel_residual;     /* largest final ||r||/||b|| over steps        */
+    double gpu_ms;               /* device time of the solve (CUDA events)      */
+    int32_t refinements;         /* mixed precision: outer sweeps, summed       */
+    int32_t graph_launches;      /* solves replayed from a captured CUDA graph  */
+    int64_t kernel_launches;     /* kernels launched by the solve               */
+    double stepper_ms;           /* device time of the time-stepping kernels    */
+} bt_stats;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int bt_version(void);
+
+/* Create a context on CUDA device `device`.  Replaces nothing in the
+ * reference: DOLFIN objects are created implicitly by the Python API
+ * (DmriFemLib.py:583-637). */
+int bt_create(bt_ctx** out, int device);
+int bt_destroy(bt_ctx* ctx);
+
+/* Copy the last error text (NUL-terminated, truncated to len). */
+int bt_last_error(const bt_ctx* ctx, char* buf, size_t len);
+
+/* Run the context's work on a caller-provided cudaStream_t (NULL restores the
+ * context's own stream). */
+int bt_set_stream(bt_ctx* ctx, void* cuda_stream);
+
+/* Upload a tetrahedral P1 mesh and build the duplicated-interface-node graph on
+ * the device (CSR + sliced-ELL, cell colouring).  Replaces DOLFIN's mesh read
+ * and function spaces: GCloudDmriSolver.py:150-152, MyFunctionSpaces
+ * (DmriFemLib.py:453-486), phase = marker % 2 (DmriFemLib.py:764).
+ *   xyz[n_vertices*3], tets[n_cells*4] (0-based), cell_region[n_cells] in
+ *   [0,n_regions), region_compartment[n_regions] (NULL: region % 2, the
+ *   reference's phase). */
+int bt_mesh_upload(bt_ctx* ctx, const double* xyz, int64_t n_vertices,
+                   const int32_t* tets, int64_t n_cells,
+                   const int32_t* cell_region, int32_t n_regions,
+                   const int32_t* region_compartment);
+
+int bt_mesh_info(bt_ctx* ctx, bt_mesh_info_t* out);
+
+/* Per-region coefficients.  D_region[n_regions] isotropic D
+ * (mydomain.D, DmriFemLib.py:611-616; GCloudDmriSolver.py:207-215);
+ * invT2_region[n_regions] 1/T2 (NULL: 0, the reference default T2=1e16,
+ * DmriFemLib.py:807); kappa_pair[n_regions*n_regions] permeability between
+ * two regions (NULL: 0; mydomain.kappa, GCloudDmriSolver.py:204, or the
+ * per-interface values of MultilayeredDiskVariablePermeability.ipynb:480-502). */
+int bt_set_coefficients(bt_ctx* ctx, const double* D_region, const double* invT2_region,
+                        const double* kappa_pair);
+
+/* Optional anisotropic per-cell D: D_cell[n_cells*6] = (xx, yy, zz, xy, xz, yz)
+ * (ImposeDiffusionTensor, DmriFemLib.py:611-616, symmetric part).  NULL
+ * clears it (back to D_region). */
+int bt_set_cell_diffusion(bt_ctx* ctx, const double* D_cell);
+
+/* Assemble M, K, T, R, Jx, Jy, Jz and the signal weights on the device with the
+ * coloured, atomic-free element kernel.  Replaces the FFC tabulate_tensor +
+ * PETSc insertion behind assemble() (DmriFemLib.py:245,252,904-905). */
+int bt_assemble(bt_ctx* ctx);
+
+/* Time schedule: f_new[n_sequences*n_steps] is f at the implicit level of
+ * each solve, f_old[...] at the explicit level, exactly as the reference's
+ * loop evaluates them (DmriFemLib.py:897-911: f(t) in F, f(tp) in L).
+ * dt = mri_simu.k, theta = mri_simu.theta. */
+int bt_set_schedule(bt_ctx* ctx, const double* f_new, const double* f_old,
+                    int32_t n_steps, int32_t n_sequences, double dt, double theta);
+
+/* Integrate n_signals Bloch-Torrey problems and return their signals.
+ *   q[n_signals]            mri_para.qvalue
+ *   gdir[n_signals*3]       unit gradient directions (set_gradient_dir)
+ *   sequence[n_signals]     schedule row of each signal (NULL: all 0)
+ *   u0[n_vertices]          initial condition (NULL: 1 everywhere, the
+ *                           reference's Dirac_Delta, DmriFemLib.py:865-876)
+ *   precision               BT_PRECISION_FP64 or BT_PRECISION_MIXED
+ *   rtol, max_iterations    per-step COCG stopping rule ||r|| <= rtol ||b||
+ *                           (linsolver relative_tolerance / maximum_iterations)
+ *   signal_out[n_signals]   int Re(u(T)) dx   (PostProcessing `signal`)
+ *   compartment_out         [n_signals*n_compartments] or NULL
+ *   S0_out                  int u0 dx         (PostProcessing `voi`)
+ * Replaces MRI_simulation.solve (DmriFemLib.py:878-915) and the signal of
+ * PostProcessing (DmriFemLib.py:922-931). */
+int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir,
+             const int32_t* sequence, const double* u0, int32_t precision,
+             double rtol, int32_t max_iterations, double* signal_out,
+             double* compartment_out, double* S0_out, bt_stats* stats);
+
+/* Introspection for tests (no counterpart in the reference). */
+int bt_get_csr(bt_ctx* ctx, int32_t* row_ptr /* n_dofs+1 */, int32_t* col /* nnz */);
+int bt_get_matrix(bt_ctx* ctx, int32_t which, double* values /* nnz */);
+int bt_get_dofs(bt_ctx* ctx, int32_t* dof_vertex, int32_t* dof_compartment, double* weights);
+int bt_get_colouring(bt_ctx* ctx, int32_t* cell_colour /* n_cells */);
+/* Final state of signal `index` of the last bt_solve: u[2*n_dofs] (re, im). */
+int bt_get_solution(bt_ctx* ctx, int32_t index, double* u);
+/* Per-step inner iteration counts of the last solve: iters[n_signals*n_steps];
+ * capacity is the number of int32 the buffer holds. */
+int bt_get_iterations(bt_ctx* ctx, int32_t* iters, int64_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BTGPU_H */
