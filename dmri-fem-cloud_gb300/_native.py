@@ -31,7 +31,7 @@ EXPORTS = [
     "bt_version", "bt_create", "bt_destroy", "bt_last_error", "bt_set_stream",
     "bt_mesh_upload", "bt_mesh_info", "bt_set_coefficients", "bt_set_cell_diffusion",
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
-    "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations",
+    "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
 ]
 
 
@@ -98,6 +98,7 @@ def load(path=None):
         "bt_get_colouring": (C.c_int, [_P, _I32]),
         "bt_get_solution": (C.c_int, [_P, C.c_int32, _D]),
         "bt_get_iterations": (C.c_int, [_P, _I32, C.c_int64]),
+        "bt_set_option": (C.c_int, [_P, C.c_char_p, C.c_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -145,6 +146,9 @@ class Context:
             buf = C.create_string_buffer(1024)
             self.lib.bt_last_error(self.h, buf, 1024)
             raise BtError(rc, buf.value.decode(errors="replace"))
+
+    def set_option(self, key, value):
+        self._check(self.lib.bt_set_option(self.h, key.encode(), float(value)))
 
     def set_stream(self, stream_ptr):
         self._check(self.lib.bt_set_stream(self.h, _P(stream_ptr) if stream_ptr else None))

@@ -263,6 +263,36 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
     });
 }
 
+int bt_set_option(bt_ctx* ctx, const char* key, double value) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(key && std::isfinite(value), BT_ERR_INVALID, "bt_set_option: bad key or value");
+        const std::string k(key);
+        const int iv = (int)value;
+        if (k == "mixed.lanes_per_row") {
+            BT_REQUIRE(iv == 0 || iv == 1 || iv == 2 || iv == 4 || iv == 8 || iv == 16 || iv == 32, BT_ERR_INVALID,
+                       "mixed.lanes_per_row must be 0 or a power of two <= 32");
+            ctx->opt_mixed_lpr = iv > 0 ? iv : -1;
+        } else if (k == "mixed.blocks_per_sm") {
+            BT_REQUIRE(iv >= 0 && iv <= 8, BT_ERR_INVALID, "mixed.blocks_per_sm must be in [0, 8]");
+            ctx->opt_mixed_blocks_per_sm = iv > 0 ? iv : -1;
+        } else if (k == "mixed.max_sweeps") {
+            BT_REQUIRE(iv >= 1 && iv <= 64, BT_ERR_INVALID, "mixed.max_sweeps must be in [1, 64]");
+            ctx->opt_mixed_max_sweeps = iv;
+        } else if (k == "mixed.eps_first") {
+            BT_REQUIRE(value > 0.0 && value < 1.0, BT_ERR_INVALID, "mixed.eps_first must be in (0, 1)");
+            ctx->opt_mixed_eps_first = value;
+        } else if (k == "mixed.eps_next") {
+            BT_REQUIRE(value > 0.0 && value < 1.0, BT_ERR_INVALID, "mixed.eps_next must be in (0, 1)");
+            ctx->opt_mixed_eps_next = value;
+        } else if (k == "fp64.extrapolate") {
+            ctx->opt_fp64_extrapolate = iv ? 1 : 0;
+        } else {
+            throw bt::Error(BT_ERR_INVALID, "bt_set_option: unknown key " + k);
+        }
+    });
+}
+
 int bt_get_csr(bt_ctx* ctx, int32_t* row_ptr, int32_t* col) {
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {

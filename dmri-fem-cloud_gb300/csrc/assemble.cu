@@ -40,6 +40,7 @@ struct AsmArgs {
     const double* invT2_region;
     const double* kappa_pair;
     double *M, *K, *T, *R, *Jx, *Jy, *Jz, *w, *vw;
+    int* status;
 };
 
 __device__ __forceinline__ int32_t find_pos(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
@@ -132,6 +133,10 @@ __global__ void k_assemble_colour(AsmArgs a) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const int32_t p = find_pos(a.row_ptr, a.col, d[r], d[c]);
+            if (p < 0) {  // inconsistent graph: record, never write out of bounds
+                atomicCAS(a.status, DEV_OK, DEV_BAD_MESH);
+                continue;
+            }
             const double m = (r == c) ? 2.0 * v20 : v20;
             a.M[p] += m;
             a.K[p] += vol * (G[r][0] * DG[c][0] + G[r][1] * DG[c][1] + G[r][2] * DG[c][2]);
@@ -181,10 +186,18 @@ __global__ void k_assemble_colour(AsmArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const double bb = (r == c) ? 2.0 * b : b;
-                a.R[find_pos(a.row_ptr, a.col, df[r], df[c])] += bb;
-                a.R[find_pos(a.row_ptr, a.col, dg[r], dg[c])] += bb;
-                a.R[find_pos(a.row_ptr, a.col, df[r], dg[c])] -= bb;
-                a.R[find_pos(a.row_ptr, a.col, dg[r], df[c])] -= bb;
+                const int32_t p0 = find_pos(a.row_ptr, a.col, df[r], df[c]);
+                const int32_t p1 = find_pos(a.row_ptr, a.col, dg[r], dg[c]);
+                const int32_t p2 = find_pos(a.row_ptr, a.col, df[r], dg[c]);
+                const int32_t p3 = find_pos(a.row_ptr, a.col, dg[r], df[c]);
+                if ((p0 | p1 | p2 | p3) < 0) {
+                    atomicCAS(a.status, DEV_OK, DEV_BAD_MESH);
+                    continue;
+                }
+                a.R[p0] += bb;
+                a.R[p1] += bb;
+                a.R[p2] -= bb;
+                a.R[p3] -= bb;
             }
     }
 }
@@ -275,6 +288,10 @@ void assemble_all(bt_ctx* ctx) {
     a.Jx = A.Jx; a.Jy = A.Jy; a.Jz = A.Jz;
     a.w = A.w;
     a.vw = A.vw;
+    DevBuf<int> status;
+    status.alloc(1);
+    status.zero(s);
+    a.status = status;
     for (int c = 0; c < m.n_colours; ++c) {
         const int32_t b = m.colour_ptr[c], e = m.colour_ptr[c + 1];
         if (e <= b) continue;
@@ -283,6 +300,10 @@ void assemble_all(bt_ctx* ctx) {
         k_assemble_colour<<<(unsigned)((a.n_cells + 127) / 128), 128, 0, s>>>(a);
         BT_CUDA(cudaGetLastError());
     }
+    int st = 0;
+    BT_CUDA(cudaMemcpyAsync(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BT_CUDA(cudaStreamSynchronize(s));
+    BT_REQUIRE(st == DEV_OK, BT_ERR_INVALID, "bt_assemble: a cell coupling is missing from the graph");
     m.volume = device_sum(A.vw, m.n_v, s);
     A.done = true;
 }

@@ -1,17 +1,1068 @@
-// Batched mixed-precision stepper (placeholder until the SpMM path lands).
+// Batched mixed-precision Crank-Nicolson stepper: up to 512 signals (gradient
+// directions, b-values, sequences) of one mesh advance together in one
+// persistent cooperative launch, as a multi-RHS SpMM over the shared CSR
+// matrices A_re = M/k + theta (K + T + R), Jx, Jy, Jz.
+//
+// Precision.  GB300 runs FP64 at a small fraction of its FP32 rate, so no
+// FP64 arithmetic is used per matrix entry.  Each time step solves the
+// correction form of the reference's step (DmriFemLib.py:901-907):
+//     A_n d = r,   r = b_n - A_n u  =  -(S u + i (cn + co) J_g u)   at u = u_n
+// where S = K + T + R and J_g = sum_k g_k J_k (theta-general: B - A = -S).
+// * u is kept as a double-float pair (hi + lo, FP32 each, ~44 bits), and the
+//   outer residual r is formed with error-free FP32 transformations (TwoProd by
+//   FMA, TwoSum) against double-float matrix values, so it is as accurate as
+//   an FP64 SpMV;
+// * the correction d is found by Jacobi-COCG entirely in FP32 (vectors and
+//   matrix hi parts), to a relative tolerance of 1e-4 in the first sweep.  The
+//   gradient winds the phase of u across the mesh, so COCG's unconjugated forms
+//   r^T z and p^T A p cancel by orders of magnitude for a complex right-hand
+//   side and FP32 COCG then stalls.  Each signal's correction is therefore
+//   solved as two right-hand sides, Re(r) and Im(r) (d = d_re + i d_im), whose
+//   Krylov vectors stay nearly real (the imaginary part of A is a few percent
+//   of its real part), and the lane-local sums are compensated (Kahan) and
+//   combined in FP64;
+// * the outer residual is updated in double-float, r -= A d, u += d, and
+//   further FP32 sweeps (tolerance 3e-3) run until ||r|| <= rtol ||b||, with
+//   ||b|| estimated as ||(1/k) w o u|| (w = lumped mass).
+// The signal int Re(u) is accumulated in FP64 at the end.
+//
+// Layout.  Inner vectors are [row][Rp] complex FP32 "slots" (slots 2s, 2s+1
+// are Re / Im of signal s; Rp a multiple of the chunk size C), so the gather of
+// a neighbour row reads C consecutive complex values: a warp-unit of LPR lanes
+// per row x (32/LPR) rows, each lane holding the 2 slots of one signal (one
+// 16-byte load per neighbour).  u and the outer residual are [row][Rp/2]
+// double-float complex per signal.  Matrix entries are loaded
+// once per unit and broadcast.  LPR ("lanes per row") and the blocks per SM
+// are chosen by a measuring autotuner (autotune_mixed).
+//
+// Reductions are deterministic: lanes sum their rows in order, warps combine
+// row slots by XOR shuffles, blocks combine warps of the same RHS chunk in
+// warp order, and the grid sums block partials in block order (in one stage
+// when the partials are few, otherwise in two stages with an extra barrier).
 #include "bt_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
 
 namespace bt {
 
-struct SolverMixed {};
+constexpr int kWarpsB = 8;
+constexpr int kThreadsB = kWarpsB * 32;
+constexpr int kMaxRhs = 512;
+constexpr int kNV = 4;  // values per RHS in one reduction
 
-void solve_mixed(bt_ctx*, int32_t, const double*, const double*, const int32_t*, const double*, double, int32_t,
-                 double*, double*, bt_stats*) {
-    throw Error(BT_ERR_INVALID, "mixed precision is not available in this build");
+struct SolverMixed {
+    int64_t n = 0;
+    int32_t Rp = 0;
+    int32_t nb = 0;
+    DevBuf<float4> mA, mL;    // per nnz: {A,Jx,Jy,Jz} hi and lo
+    DevBuf<float2> mS;        // per nnz: S hi, lo
+    DevBuf<float4> dg;        // per row: diagonal {A,Jx,Jy,Jz} (hi)
+    DevBuf<double> w;         // per row signal weight
+    DevBuf<int32_t> rcomp;
+    DevBuf<float2> uh, ul, rh, rl, d0, d1, ri, z, p, q;  // [n][Rp]
+    DevBuf<double> partials, fin;
+    DevBuf<double> sigpart;      // [warps][64][1+kMaxCompartments]
+    DevBuf<unsigned> bar;
+    DevBuf<int> status;
+    DevBuf<double> fnew, fold;   // [n_seq][n_steps]
+    DevBuf<double> qv;           // [Rp]
+    DevBuf<float> gv;            // [Rp][3]
+    DevBuf<int32_t> seqv;        // [Rp]
+    DevBuf<double> sig;          // [Rp][1 + kMaxCompartments]
+    DevBuf<int32_t> iters, sweeps;  // [n_steps]
+    DevBuf<float> diag;
+    DevBuf<double> u0;
+    // final solutions of the last solve: [nsig][n] complex (hi + lo, as double2)
+    std::vector<double2> saved;
+    int32_t saved_nsig = 0;
+    std::map<std::pair<int64_t, int32_t>, std::pair<int, int>> tuned;  // (n,Rp) -> (LPR, blocks/SM)
+};
+
+struct MixArgs {
+    int32_t n;
+    int32_t Rp;
+    int32_t R;            // real RHS (the rest is padding)
+    const int32_t* __restrict__ row_ptr;
+    const int32_t* __restrict__ col;
+    const float4* __restrict__ mA;
+    const float4* __restrict__ mL;
+    const float2* __restrict__ mS;
+    const float4* __restrict__ dg;
+    const double* __restrict__ w;
+    const int32_t* __restrict__ rcomp;
+    float2* uh;  // per signal: [row][Rp/2] complex (double-float hi / lo)
+    float2* ul;
+    float2* rh;
+    float2* rl;
+    float4* dv[2];
+    float4* ri;
+    float4* z;
+    float4* p;
+    float4* q;
+    double* partials;
+    double* fin;
+    double* sigpart;
+    unsigned* bar;
+    int* status;
+    const double* __restrict__ fnew;
+    const double* __restrict__ fold;
+    const double* __restrict__ qv;
+    const float* __restrict__ gv;
+    const int32_t* __restrict__ seqv;
+    int32_t n_steps;
+    int32_t sched_stride;  // steps per schedule row (n_steps may be fewer when tuning)
+    int32_t maxit;
+    int32_t max_sweeps;
+    float theta;
+    float inv_k;
+    float rtol;
+    float eps_first;
+    float eps_next;
+    int32_t two_stage;
+    int32_t* iters;
+    int32_t* sweeps;
+    double* sig;  // [Rp][1+kMaxCompartments]
+    float* diag;  // failure report: kind, step, sweep, iteration, worst rr2/target, RHS
+};
+
+// ------------------------------------------------------------ double-float ----
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
 }
-void get_solution_mixed(bt_ctx*, int32_t, double*) {
-    throw Error(BT_ERR_INVALID, "mixed precision is not available in this build");
+// acc += (ah + al) * (xh + xl), error-free product of the hi parts
+__device__ __forceinline__ void df_fma(DF& acc, float ah, float al, float xh, float xl) {
+    const float p = ah * xh;
+    float e = fmaf(ah, xh, -p);
+    e = fmaf(ah, xl, e);
+    e = fmaf(al, xh, e);
+    float s, t;
+    two_sum(acc.h, p, s, t);
+    acc.h = s;
+    acc.l += t + e;
 }
+__device__ __forceinline__ DF df_norm(DF a) {
+    DF r;
+    r.h = a.h + a.l;
+    r.l = a.l - (r.h - a.h);
+    return r;
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    e += a.l + b.l;
+    DF r;
+    r.h = s + e;
+    r.l = e - (r.h - s);
+    return r;
+}
+__device__ __forceinline__ DF df_scale(DF a, float c) {
+    const float p = a.h * c;
+    const float e = fmaf(a.h, c, -p);
+    DF r;
+    r.h = p;
+    r.l = fmaf(a.l, c, e);
+    return df_norm(r);
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// Smith's complex division: no squared magnitudes, so FP32 COCG scalars that
+// are themselves sums of squared residuals (~1e-25) neither underflow nor
+// overflow here.
+__device__ __forceinline__ float2 cdivf(float2 a, float2 b) {
+    if (fabsf(b.x) >= fabsf(b.y)) {
+        const float r = b.y / b.x, d = fmaf(b.y, r, b.x);
+        return make_float2(fmaf(a.y, r, a.x) / d, fmaf(-a.x, r, a.y) / d);
+    }
+    const float r = b.x / b.y, d = fmaf(b.x, r, b.y);
+    return make_float2(fmaf(a.x, r, a.y) / d, fmaf(a.y, r, -a.x) / d);
+}
+__device__ __forceinline__ float2 cinvf(float2 b) { return cdivf(make_float2(1.0f, 0.0f), b); }
+__device__ __forceinline__ bool cnonzero(float2 v) {
+    return (v.x != 0.0f || v.y != 0.0f) && isfinite(v.x) && isfinite(v.y);
+}
+__device__ __forceinline__ bool cnonzero(double2 v) {
+    return (v.x != 0.0 || v.y != 0.0) && isfinite(v.x) && isfinite(v.y);
+}
+__device__ __forceinline__ float2 cdivf_d(double2 a, double2 b) {  // FP64 Smith division, FP32 result
+    if (fabs(b.x) >= fabs(b.y)) {
+        const double r = b.y / b.x, d = fma(b.y, r, b.x);
+        return make_float2((float)(fma(a.y, r, a.x) / d), (float)(fma(-a.x, r, a.y) / d));
+    }
+    const double r = b.x / b.y, d = fma(b.x, r, b.y);
+    return make_float2((float)(fma(a.x, r, a.y) / d), (float)(fma(a.y, r, -a.x) / d));
+}
+
+// Compensated (Kahan) FP32 accumulator.  The COCG scalars are sums of
+// products whose phases wind across the mesh (the gradient encodes position in
+// the phase), so they cancel by orders of magnitude; plain FP32 sequential sums
+// then lose the step length and COCG stalls.  Lanes accumulate compensated,
+// and every combination above the lane is done in FP64.
+struct KF {
+    float s, c;
+};
+__device__ __forceinline__ void kadd(KF& a, float x) {
+    const float y = x - a.c;
+    const float t = a.s + y;
+    a.c = (t - a.s) - y;
+    a.s = t;
+}
+
+// -------------------------------------------------------------- reductions ----
+// Each lane holds compensated sums v[2][kNV] for its two RHS.  On return out[][]
+// holds the grid-wide sums (FP64) for those RHS, bitwise identical in every block.
+template <int LPR>
+__device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], double (&out)[2][kNV], const MixArgs& a, int chunk,
+                                           int r0, unsigned nb, unsigned& gen, double* smem) {
+    constexpr int C = 2 * LPR;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    double d[2][kNV];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int k = 0; k < kNV; ++k) d[j][k] = (double)v[j][k].s - (double)v[j][k].c;
+    // combine the row slots of the warp
+#pragma unroll
+    for (int o = 16; o >= LPR; o >>= 1) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV; ++k) d[j][k] += __shfl_xor_sync(0xffffffffu, d[j][k], o);
+    }
+    if (lane < LPR) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV; ++k) smem[(wib * C + lane * 2 + j) * kNV + k] = d[j][k];
+    }
+    __syncthreads();
+    const int nchunks = a.Rp / C;
+    // block partial for every RHS: sum over this block's warps of that chunk, in order
+    for (int t = threadIdx.x; t < a.Rp * kNV; t += blockDim.x) {
+        const int r = t / kNV, k = t % kNV;
+        const int c = r / C, o = r % C;
+        double s = 0.0;
+        for (int wb = 0; wb < kWarpsB; ++wb)
+            if ((int)((blockIdx.x * kWarpsB + wb) % nchunks) == c) s += smem[(wb * C + o) * kNV + k];
+        a.partials[(size_t)blockIdx.x * a.Rp * kNV + t] = s;
+    }
+    if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
+    if (a.two_stage) {
+        // stage 2: grid threads each finish some (r, k) in block order
+        const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+        for (int t = gt; t < a.Rp * kNV; t += nb * blockDim.x) {
+            double s = 0.0;
+            for (unsigned b = 0; b < nb; ++b) s += __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]);
+            a.fin[t] = s;
+        }
+        if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV; ++k) out[j][k] = __ldcg(&a.fin[(r0 + j) * kNV + k]);
+    } else {
+        // one stage: each block sums all partials (few) into shared memory
+        __syncthreads();
+        for (int t = threadIdx.x; t < a.Rp * kNV; t += blockDim.x) {
+            double s = 0.0;
+            for (unsigned b = 0; b < nb; ++b) s += __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]);
+            smem[t] = s;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV; ++k) out[j][k] = smem[(r0 + j) * kNV + k];
+    }
+    __syncthreads();
+    return true;
+}
+
+// ------------------------------------------------------------------ kernel ----
+template <int LPR>
+__global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
+    constexpr int G = 32 / LPR;  // rows per warp-unit
+    constexpr int C = 2 * LPR;   // RHS per warp-unit
+    __shared__ double smem[kWarpsB * 64 * kNV > kMaxRhs * kNV ? kWarpsB * 64 * kNV : kMaxRhs * kNV];
+    __shared__ int s_flag;
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kWarpsB + (threadIdx.x >> 5);
+    const int total_warps = gridDim.x * kWarpsB;
+    const unsigned nb = gridDim.x;
+    const int nchunks = a.Rp / C;
+    const int chunk = gw % nchunks;
+    const int slot = lane / LPR;
+    const int r0 = chunk * C + (lane % LPR) * 2;  // this lane's first RHS
+    const int c4 = r0 >> 1;                        // float4 index of the lane's 2 RHS inside a row
+    const int Rp4 = a.Rp >> 1;                     // float4 per row
+    const int ngroups = (a.n + G - 1) / G;
+    const int g0 = gw / nchunks, gstride = total_warps / nchunks;
+    unsigned gen = 0;
+    // per-lane RHS parameters
+    double qd[2];
+    float gx[2], gy[2], gz[2];
+    int sq[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        qd[j] = a.qv[r0 + j];
+        gx[j] = a.gv[(r0 + j) * 3 + 0];
+        gy[j] = a.gv[(r0 + j) * 3 + 1];
+        gz[j] = a.gv[(r0 + j) * 3 + 2];
+        sq[j] = a.seqv[r0 + j];
+    }
+    // partial buffers alternate between consecutive reductions (see reduce_rhs)
+    double* const part0 = a.partials;
+    double* const part1 = a.partials + (size_t)nb * a.Rp * kNV;
+    unsigned flip = 0;
+    MixArgs b = a;
+#define BT_REDUCE(V, OUT)                                                     \
+    do {                                                                      \
+        b.partials = (flip++ & 1u) ? part1 : part0;                           \
+        if (!reduce_rhs<LPR>(V, OUT, b, chunk, r0, nb, gen, smem)) return;    \
+    } while (0)
+
+    int dsel = 0;
+    for (int step = 0; step < a.n_steps; ++step) {
+        float cn[2], cs[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const double fnv = a.fnew[(size_t)sq[j] * a.sched_stride + step];
+            const double fov = a.fold[(size_t)sq[j] * a.sched_stride + step];
+            cn[j] = (float)(a.theta * qd[j] * fnv);
+            cs[j] = (float)(a.theta * qd[j] * fnv + (1.0 - a.theta) * qd[j] * fov);  // cn + co
+        }
+        // ---- phase S: r = -(S u + i (cn+co) Jg u) in double-float for the lane's
+        //      signal; the FP32 inner solve starts from Re(r) (slot 0) and Im(r) (slot 1)
+        KF red[2][kNV];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV; ++k) red[j][k] = KF{0.0f, 0.0f};
+        for (int g = g0; g < ngroups; g += gstride) {
+            const int row = g * G + slot;
+            if (row >= a.n) continue;
+            DF sr[2], jx[2], jy[2], jz[2];  // [re/im]
+#pragma unroll
+            for (int c = 0; c < 2; ++c) sr[c] = jx[c] = jy[c] = jz[c] = DF{0.0f, 0.0f};
+            const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
+            for (int e = e0; e < e1; ++e) {
+                const int cidx = a.col[e];
+                const float2 s2 = a.mS[e];
+                const float4 hi = a.mA[e], lo = a.mL[e];
+                const float2 uh = a.uh[(size_t)cidx * Rp4 + c4];
+                const float2 ul = a.ul[(size_t)cidx * Rp4 + c4];
+                const float uhv[2] = {uh.x, uh.y}, ulv[2] = {ul.x, ul.y};
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    df_fma(sr[c], s2.x, s2.y, uhv[c], ulv[c]);
+                    df_fma(jx[c], hi.y, lo.y, uhv[c], ulv[c]);
+                    df_fma(jy[c], hi.z, lo.z, uhv[c], ulv[c]);
+                    df_fma(jz[c], hi.w, lo.w, uhv[c], ulv[c]);
+                }
+            }
+            const float4 dgr = a.dg[row];
+            const float wr = (float)a.w[row] * a.inv_k;
+            const size_t vi = (size_t)row * Rp4 + c4;
+            const float2 uhr = a.uh[vi];
+            DF jg[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+                jg[c] = df_add(df_add(df_scale(df_norm(jx[c]), gx[0]), df_scale(df_norm(jy[c]), gy[0])),
+                               df_scale(df_norm(jz[c]), gz[0]));
+            // -i cs (a + i b) = cs b - i cs a
+            const DF re = df_add(df_neg(df_norm(sr[0])), df_scale(jg[1], cs[0]));
+            const DF im = df_add(df_neg(df_norm(sr[1])), df_scale(jg[0], -cs[0]));
+            a.rh[vi] = make_float2(re.h, im.h);
+            a.rl[vi] = make_float2(re.l, im.l);
+            const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
+            const float2 z0 = make_float2(dinv.x * re.h, dinv.y * re.h);
+            const float2 z1 = make_float2(dinv.x * im.h, dinv.y * im.h);
+            a.ri[vi] = make_float4(re.h, 0.f, im.h, 0.f);
+            a.z[vi] = make_float4(z0.x, z0.y, z1.x, z1.y);
+            a.p[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
+            a.q[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
+            a.dv[dsel][vi] = make_float4(0.f, 0.f, 0.f, 0.f);
+            kadd(red[0][0], re.h * z0.x);
+            kadd(red[0][1], re.h * z0.y);
+            kadd(red[0][2], re.h * re.h);
+            kadd(red[1][0], im.h * z1.x);
+            kadd(red[1][1], im.h * z1.y);
+            kadd(red[1][2], im.h * im.h);
+            const float bn = wr * wr * (uhr.x * uhr.x + uhr.y * uhr.y);
+            kadd(red[0][3], bn);
+            kadd(red[1][3], bn);
+        }
+        double rs[2][kNV];
+        BT_REDUCE(red, rs);
+        double2 rho[2];
+        double rr2[2], tolb2[2], rrs[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            rho[j] = make_double2(rs[j][0], rs[j][1]);
+            rr2[j] = rs[j][2];
+            rrs[j] = rs[j][2];
+            tolb2[j] = (double)a.rtol * (double)a.rtol * rs[j][3];   // (rtol ||b||)^2
+        }
+        int sweep = 0, it_total = 0;
+        bool failed = false;
+        while (true) {
+            // ---- inner FP32 Jacobi-COCG on A d = r (sweep start residual rrs)
+            const float eps = (sweep == 0) ? a.eps_first : a.eps_next;
+            float2 beta[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            bool act[2];
+            int it = 0;
+            while (true) {
+                // lane-local activity of its two RHS; grid decision via s_flag below
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                    act[j] = (r0 + j < a.R) && rr2[j] > (double)eps * eps * rrs[j] && rr2[j] > 0.09 * tolb2[j];
+                if (threadIdx.x == 0) s_flag = 0;
+                __syncthreads();
+                if (act[0] || act[1]) s_flag = 1;
+                __syncthreads();
+                // every block sees the same rr2/rrs (grid-identical sums), so s_flag is uniform
+                if (!s_flag) break;
+                if (it >= a.maxit) {
+                    if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
+#pragma unroll
+                    for (int j = 0; j < 2; ++j)
+                        if (blockIdx.x == 0 && act[j]) {
+                            a.diag[0] = 1.0f; a.diag[1] = (float)step; a.diag[2] = (float)sweep; a.diag[3] = (float)it;
+                            a.diag[4] = (float)(rr2[j] / fmax((double)eps * eps * rrs[j], 1e-300));
+                            a.diag[5] = (float)(r0 / 2);
+                        }
+                    failed = true;
+                    break;
+                }
+                // phase A: w = A z ; q = w + beta q ; p = z + beta p ; mu = p^T q
+                KF mu[2][kNV];
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+#pragma unroll
+                    for (int k = 0; k < kNV; ++k) mu[j][k] = KF{0.0f, 0.0f};
+                for (int g = g0; g < ngroups; g += gstride) {
+                    const int row = g * G + slot;
+                    if (row >= a.n) continue;
+                    float2 sA[2], sx[2], sy[2], sz[2];
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) sA[j] = sx[j] = sy[j] = sz[j] = make_float2(0.f, 0.f);
+                    const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
+                    for (int e = e0; e < e1; ++e) {
+                        const int cidx = a.col[e];
+                        const float4 m = a.mA[e];
+                        const float4 zz = a.z[(size_t)cidx * Rp4 + c4];
+                        const float2 zj[2] = {make_float2(zz.x, zz.y), make_float2(zz.z, zz.w)};
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            sA[j].x = fmaf(m.x, zj[j].x, sA[j].x); sA[j].y = fmaf(m.x, zj[j].y, sA[j].y);
+                            sx[j].x = fmaf(m.y, zj[j].x, sx[j].x); sx[j].y = fmaf(m.y, zj[j].y, sx[j].y);
+                            sy[j].x = fmaf(m.z, zj[j].x, sy[j].x); sy[j].y = fmaf(m.z, zj[j].y, sy[j].y);
+                            sz[j].x = fmaf(m.w, zj[j].x, sz[j].x); sz[j].y = fmaf(m.w, zj[j].y, sz[j].y);
+                        }
+                    }
+                    const size_t vi = (size_t)row * Rp4 + c4;
+                    const float4 zo = a.z[vi], po = a.p[vi], qo = a.q[vi];
+                    const float zov[4] = {zo.x, zo.y, zo.z, zo.w}, pov[4] = {po.x, po.y, po.z, po.w},
+                                qov[4] = {qo.x, qo.y, qo.z, qo.w};
+                    float pn[4], qn[4];
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const float jr = gx[j] * sx[j].x + gy[j] * sy[j].x + gz[j] * sz[j].x;
+                        const float ji = gx[j] * sx[j].y + gy[j] * sy[j].y + gz[j] * sz[j].y;
+                        const float2 wv = make_float2(fmaf(-cn[j], ji, sA[j].x), fmaf(cn[j], jr, sA[j].y));
+                        const float2 bp = cmulf(beta[j], make_float2(pov[2 * j], pov[2 * j + 1]));
+                        const float2 bq = cmulf(beta[j], make_float2(qov[2 * j], qov[2 * j + 1]));
+                        pn[2 * j] = zov[2 * j] + bp.x;
+                        pn[2 * j + 1] = zov[2 * j + 1] + bp.y;
+                        qn[2 * j] = wv.x + bq.x;
+                        qn[2 * j + 1] = wv.y + bq.y;
+                        const float2 pq = cmulf(make_float2(pn[2 * j], pn[2 * j + 1]), make_float2(qn[2 * j], qn[2 * j + 1]));
+                        kadd(mu[j][0], pq.x);
+                        kadd(mu[j][1], pq.y);
+                    }
+                    a.p[vi] = make_float4(pn[0], pn[1], pn[2], pn[3]);
+                    a.q[vi] = make_float4(qn[0], qn[1], qn[2], qn[3]);
+                }
+                double ms[2][kNV];
+                BT_REDUCE(mu, ms);
+                float2 alpha[2];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const double2 m2 = make_double2(ms[j][0], ms[j][1]);
+                    // inactive or broken-down RHS take no step (its residual stays put;
+                    // the outer check reports it if it never converges)
+                    alpha[j] = (act[j] && cnonzero(m2) && cnonzero(rho[j])) ? cdivf_d(rho[j], m2)
+                                                                           : make_float2(0.f, 0.f);
+                }
+                // phase B: d += alpha p ; r -= alpha q ; z = D^-1 r
+                KF rb[2][kNV];
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+#pragma unroll
+                    for (int k = 0; k < kNV; ++k) rb[j][k] = KF{0.0f, 0.0f};
+                for (int g = g0; g < ngroups; g += gstride) {
+                    const int row = g * G + slot;
+                    if (row >= a.n) continue;
+                    const size_t vi = (size_t)row * Rp4 + c4;
+                    const float4 pv = a.p[vi], qv = a.q[vi], dv = a.dv[dsel][vi], rv = a.ri[vi];
+                    const float4 dgr = a.dg[row];
+                    const float pvv[4] = {pv.x, pv.y, pv.z, pv.w}, qvv[4] = {qv.x, qv.y, qv.z, qv.w};
+                    float dn[4] = {dv.x, dv.y, dv.z, dv.w}, rn[4] = {rv.x, rv.y, rv.z, rv.w}, zn[4];
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const float2 ap = cmulf(alpha[j], make_float2(pvv[2 * j], pvv[2 * j + 1]));
+                        const float2 aq = cmulf(alpha[j], make_float2(qvv[2 * j], qvv[2 * j + 1]));
+                        dn[2 * j] += ap.x;
+                        dn[2 * j + 1] += ap.y;
+                        rn[2 * j] -= aq.x;
+                        rn[2 * j + 1] -= aq.y;
+                        const float2 dinv =
+                            cinvf(make_float2(dgr.x, cn[j] * (gx[j] * dgr.y + gy[j] * dgr.z + gz[j] * dgr.w)));
+                        const float2 zz = cmulf(dinv, make_float2(rn[2 * j], rn[2 * j + 1]));
+                        zn[2 * j] = zz.x;
+                        zn[2 * j + 1] = zz.y;
+                        const float2 rz = cmulf(make_float2(rn[2 * j], rn[2 * j + 1]), zz);
+                        kadd(rb[j][0], rz.x);
+                        kadd(rb[j][1], rz.y);
+                        kadd(rb[j][2], rn[2 * j] * rn[2 * j] + rn[2 * j + 1] * rn[2 * j + 1]);
+                    }
+                    a.dv[dsel][vi] = make_float4(dn[0], dn[1], dn[2], dn[3]);
+                    a.ri[vi] = make_float4(rn[0], rn[1], rn[2], rn[3]);
+                    a.z[vi] = make_float4(zn[0], zn[1], zn[2], zn[3]);
+                }
+                double rbs[2][kNV];
+                BT_REDUCE(rb, rbs);
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const double2 rn2 = make_double2(rbs[j][0], rbs[j][1]);
+                    beta[j] = (act[j] && cnonzero(rho[j])) ? cdivf_d(rn2, rho[j]) : make_float2(0.f, 0.f);
+                    if (act[j]) {
+                        rho[j] = rn2;
+                        rr2[j] = rbs[j][2];
+                    }
+                }
+                ++it;
+            }
+            it_total += it;
+            if (failed) break;
+            // ---- phase U: d = d_re-part + i d_im-part ; u += d ; r -= A d (double-float);
+            //      restart the inner slots from Re(r), Im(r)
+            KF ru[2][kNV];
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int k = 0; k < kNV; ++k) ru[j][k] = KF{0.0f, 0.0f};
+            for (int g = g0; g < ngroups; g += gstride) {
+                const int row = g * G + slot;
+                if (row >= a.n) continue;
+                DF ar[2], jx[2], jy[2], jz[2];
+#pragma unroll
+                for (int c = 0; c < 2; ++c) ar[c] = jx[c] = jy[c] = jz[c] = DF{0.0f, 0.0f};
+                const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
+                for (int e = e0; e < e1; ++e) {
+                    const int cidx = a.col[e];
+                    const float4 hi = a.mA[e], lo = a.mL[e];
+                    const float4 dd = a.dv[dsel][(size_t)cidx * Rp4 + c4];
+                    const float dc[2] = {dd.x - dd.w, dd.y + dd.z};  // d0 + i d1
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        df_fma(ar[c], hi.x, lo.x, dc[c], 0.0f);
+                        df_fma(jx[c], hi.y, lo.y, dc[c], 0.0f);
+                        df_fma(jy[c], hi.z, lo.z, dc[c], 0.0f);
+                        df_fma(jz[c], hi.w, lo.w, dc[c], 0.0f);
+                    }
+                }
+                const size_t vi = (size_t)row * Rp4 + c4;
+                const float4 dgr = a.dg[row];
+                const float2 rh = a.rh[vi], rl = a.rl[vi], uh = a.uh[vi], ul = a.ul[vi];
+                const float4 dd = a.dv[dsel][vi];
+                const float dco[2] = {dd.x - dd.w, dd.y + dd.z};
+                DF jg[2];
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+                    jg[c] = df_add(df_add(df_scale(df_norm(jx[c]), gx[0]), df_scale(df_norm(jy[c]), gy[0])),
+                                   df_scale(df_norm(jz[c]), gz[0]));
+                // A d = A_re d + i cn Jg d
+                const DF adr = df_add(df_norm(ar[0]), df_scale(jg[1], -cn[0]));
+                const DF adi = df_add(df_norm(ar[1]), df_scale(jg[0], cn[0]));
+                const DF nr = df_add(DF{rh.x, rl.x}, df_neg(adr));
+                const DF ni = df_add(DF{rh.y, rl.y}, df_neg(adi));
+                const DF u_re = df_add(DF{uh.x, ul.x}, DF{dco[0], 0.0f});
+                const DF u_im = df_add(DF{uh.y, ul.y}, DF{dco[1], 0.0f});
+                a.rh[vi] = make_float2(nr.h, ni.h);
+                a.rl[vi] = make_float2(nr.l, ni.l);
+                a.uh[vi] = make_float2(u_re.h, u_im.h);
+                a.ul[vi] = make_float2(u_re.l, u_im.l);
+                const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
+                const float2 z0 = make_float2(dinv.x * nr.h, dinv.y * nr.h);
+                const float2 z1 = make_float2(dinv.x * ni.h, dinv.y * ni.h);
+                a.ri[vi] = make_float4(nr.h, 0.f, ni.h, 0.f);
+                a.z[vi] = make_float4(z0.x, z0.y, z1.x, z1.y);
+                a.p[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
+                a.q[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
+                a.dv[dsel ^ 1][vi] = make_float4(0.f, 0.f, 0.f, 0.f);
+                kadd(ru[0][0], nr.h * z0.x);
+                kadd(ru[0][1], nr.h * z0.y);
+                kadd(ru[0][2], nr.h * nr.h);
+                kadd(ru[1][0], ni.h * z1.x);
+                kadd(ru[1][1], ni.h * z1.y);
+                kadd(ru[1][2], ni.h * ni.h);
+            }
+            double rus[2][kNV];
+            BT_REDUCE(ru, rus);
+            dsel ^= 1;
+            ++sweep;
+            bool more = false;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                rho[j] = make_double2(rus[j][0], rus[j][1]);
+                rr2[j] = rus[j][2];
+                rrs[j] = rus[j][2];
+            }
+            // the lane's two slots are Re and Im of one signal: ||r||^2 = sum of both
+            if (r0 < a.R && rr2[0] + rr2[1] > tolb2[0]) more = true;
+            if (threadIdx.x == 0) s_flag = 0;
+            __syncthreads();
+            if (more) s_flag = 1;
+            __syncthreads();
+            if (!s_flag) break;
+            if (sweep >= a.max_sweeps) {
+                if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
+                if (blockIdx.x == 0 && r0 < a.R && rr2[0] + rr2[1] > tolb2[0]) {
+                    a.diag[0] = 2.0f; a.diag[1] = (float)step; a.diag[2] = (float)sweep; a.diag[3] = (float)it_total;
+                    a.diag[4] = (float)((rr2[0] + rr2[1]) / fmax(tolb2[0], 1e-300)); a.diag[5] = (float)(r0 / 2);
+                }
+                failed = true;
+                break;
+            }
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.iters[step] = it_total;
+            a.sweeps[step] = sweep;
+        }
+        if (failed) return;
+    }
+#undef BT_REDUCE
+    // ---- signal: FP64 sums of w Re(u) per RHS and compartment (lanes own their RHS)
+    double acc[2][1 + kMaxCompartments];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int k = 0; k <= kMaxCompartments; ++k) acc[j][k] = 0.0;
+    for (int g = g0; g < ngroups; g += gstride) {
+        const int row = g * G + slot;
+        if (row >= a.n) continue;
+        const size_t vi = (size_t)row * Rp4 + c4;
+        const float2 uh = a.uh[vi], ul = a.ul[vi];
+        const double wr = a.w[row];
+        const int cm = a.rcomp[row];
+        const double v0 = wr * ((double)uh.x + (double)ul.x);
+        acc[0][0] += v0;
+#pragma unroll
+        for (int k = 0; k < kMaxCompartments; ++k)
+            if (k == cm) acc[0][1 + k] += v0;
+    }
+    // deterministic: combine the row slots by shuffles, stage per-warp partials,
+    // then sum the warps of each RHS chunk in warp order
+#pragma unroll
+    for (int o = 16; o >= LPR; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k <= kMaxCompartments; ++k) acc[j][k] += __shfl_xor_sync(0xffffffffu, acc[j][k], o);
+    double* wp = a.sigpart;  // [total_warps][C][1+kMaxCompartments], not shared with the reductions
+    if (lane < LPR) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k <= kMaxCompartments; ++k)
+                wp[((size_t)gw * C + lane * 2 + j) * (1 + kMaxCompartments) + k] = acc[j][k];
+    }
+    if (!grid_barrier(a.bar, nb, a.status, gen)) return;
+    // grid thread t finishes (RHS r, value k): sum over warps of r's chunk in warp order
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int t = gt; t < a.Rp * (1 + kMaxCompartments); t += nb * blockDim.x) {
+        const int r = t / (1 + kMaxCompartments), k = t % (1 + kMaxCompartments);
+        const int c = r / C, o = r % C;
+        double s = 0.0;
+        for (int wv = c; wv < total_warps; wv += nchunks)
+            s += __ldcg(&wp[((size_t)wv * C + o) * (1 + kMaxCompartments) + k]);
+        a.sig[t] = s;
+    }
+}
+
+// Pack the double-float matrix copies and the row data once per assembly/theta/dt.
+__global__ void k_pack_mixed(int64_t nnz, const double* __restrict__ M, const double* __restrict__ K,
+                             const double* __restrict__ T, const double* __restrict__ R,
+                             const double* __restrict__ Jx, const double* __restrict__ Jy,
+                             const double* __restrict__ Jz, double inv_k, double theta, float4* __restrict__ mA,
+                             float4* __restrict__ mL, float2* __restrict__ mS) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnz) return;
+    const double S = K[e] + T[e] + R[e];
+    const double A = M[e] * inv_k + theta * S;
+    const double v[4] = {A, Jx[e], Jy[e], Jz[e]};
+    float h[4], l[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        h[k] = (float)v[k];
+        l[k] = (float)(v[k] - (double)h[k]);
+    }
+    mA[e] = make_float4(h[0], h[1], h[2], h[3]);
+    mL[e] = make_float4(l[0], l[1], l[2], l[3]);
+    const float sh = (float)S;
+    mS[e] = make_float2(sh, (float)(S - (double)sh));
+}
+
+__global__ void k_rows_mixed(int64_t n, int32_t Rp, int32_t R, const int32_t* __restrict__ diag_pos,
+                             const float4* __restrict__ mA, const double* __restrict__ wsrc,
+                             const int32_t* __restrict__ comp, const int32_t* __restrict__ dof_vertex,
+                             const double* __restrict__ u0, float4* __restrict__ dg, double* __restrict__ w,
+                             int32_t* __restrict__ rcomp, float2* __restrict__ uh, float2* __restrict__ ul) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dg[i] = mA[diag_pos[i]];
+    w[i] = wsrc[i];
+    rcomp[i] = comp[i];
+    const double v = u0 ? u0[dof_vertex[i]] : 1.0;
+    const float h = (float)v;
+    const float l = (float)(v - (double)h);
+    const int ns = Rp / 2;  // signals per row: slots 2s, 2s+1 are Re / Im parts of signal s
+    for (int sg = 0; sg < ns; ++sg) {
+        const bool live = 2 * sg < R;
+        uh[(size_t)i * ns + sg] = make_float2(live ? h : 0.f, 0.f);
+        ul[(size_t)i * ns + sg] = make_float2(live ? l : 0.f, 0.f);
+    }
+}
+
+namespace {
+
+using KFn = void (*)(MixArgs);
+
+KFn kernel_for(int lpr) {
+    switch (lpr) {
+        case 1: return k_batched<1>;
+        case 2: return k_batched<2>;
+        case 4: return k_batched<4>;
+        case 8: return k_batched<8>;
+        case 16: return k_batched<16>;
+        default: return k_batched<32>;
+    }
+}
+
+int ceil_pow2(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// Padded RHS count for chunk C = 2*LPR: the number of chunks is rounded up to
+// a power of two <= 8, so every block of 8 warps covers every chunk equally.
+int padded_rhs(int R, int lpr) {
+    const int C = 2 * lpr;
+    const int nch = ceil_pow2((R + C - 1) / C);
+    return (nch <= kWarpsB) ? C * nch : -1;
+}
+
+// Valid lanes-per-row for a batch of R: C = 2*LPR no larger than the padded
+// batch needs, and at most 8 chunks.
+std::vector<int> lpr_candidates(int R) {
+    std::vector<int> out;
+    const int Rp2 = std::max(2, ceil_pow2(R));
+    for (int lpr = 1; lpr <= 32; lpr <<= 1) {
+        if (2 * lpr > Rp2) break;
+        if (padded_rhs(R, lpr) > 0) out.push_back(lpr);
+    }
+    return out;
+}
+
+}  // namespace
+
+static void map_status_mixed(int st) {
+    switch (st) {
+        case DEV_OK: return;
+        case DEV_TIMEOUT: throw Error(BT_ERR_TIMEOUT, "mixed stepper: a grid barrier wait ran out of time");
+        case DEV_NOT_CONVERGED:
+            throw Error(BT_ERR_NOT_CONVERGED, "mixed stepper: inner COCG or refinement did not converge");
+        default: throw Error(BT_ERR_CUDA, "mixed stepper: device status " + std::to_string(st));
+    }
+}
+
+// Launch one batch (R <= 512 signals) with the given geometry; n_steps may be
+// truncated for tuning.  Returns the device time of the stepper kernel (ms).
+static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int n_steps, double rtol,
+                          int maxit, const double* d_u0) {
+    Mesh& m = ctx->mesh;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    BT_REQUIRE(R >= 1 && R <= kMaxRhs && (lpr == 1 || lpr == 2 || lpr == 4 || lpr == 8 || lpr == 16 || lpr == 32),
+               BT_ERR_INVALID, "mixed stepper: invalid batch geometry");
+    const int Rp = padded_rhs(R, lpr);
+    BT_REQUIRE(Rp >= R && Rp <= kMaxRhs && (Rp / (2 * lpr)) <= kWarpsB && (kWarpsB % (Rp / (2 * lpr))) == 0,
+               BT_ERR_INVALID, "mixed stepper: invalid RHS padding");
+    KFn fn = kernel_for(lpr);
+    int occ = 0;
+    BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
+    BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
+    const int per_sm = std::max(1, std::min(occ, per_sm_blocks));
+    const int G = 32 / lpr;
+    const int units = (int)(((m.n_dofs + G - 1) / G) * (Rp / (2 * lpr)));
+    const int need = std::max(1, (units + kWarpsB - 1) / kWarpsB);
+    const int nb = std::max(1, std::min(per_sm * ctx->num_sms, need));
+    // partials: two alternating float buffers [nb][Rp][kNV]
+    W.partials.alloc((size_t)2 * nb * Rp * kNV);
+    W.sigpart.alloc((size_t)nb * kWarpsB * 64 * (1 + kMaxCompartments));
+    W.fin.alloc((size_t)Rp * kNV);
+    const size_t nv = (size_t)m.n_dofs * Rp;
+    for (auto* v : {&W.d0, &W.d1, &W.ri, &W.z, &W.p, &W.q}) v->alloc(nv);        // per slot
+    for (auto* v : {&W.uh, &W.ul, &W.rh, &W.rl}) v->alloc(nv / 2);               // per signal
+    W.sig.alloc((size_t)Rp * (1 + kMaxCompartments));
+    W.bar.alloc(2);
+    W.status.alloc(1);
+    W.diag.alloc(8);
+    W.diag.zero(s);
+    k_rows_mixed<<<(unsigned)((m.n_dofs + 255) / 256), 256, 0, s>>>(m.n_dofs, Rp, R, m.diag_pos, W.mA, ctx->mat.w,
+                                                                    m.dof_comp, m.dof_vertex, d_u0, W.dg, W.w,
+                                                                    W.rcomp, W.uh, W.ul);
+    BT_CUDA(cudaGetLastError());
+    W.bar.zero(s);
+    W.status.zero(s);
+    MixArgs a;
+    a.n = (int32_t)m.n_dofs;
+    a.Rp = Rp;
+    a.R = R;
+    a.row_ptr = m.row_ptr;
+    a.col = m.col;
+    a.mA = W.mA;
+    a.mL = W.mL;
+    a.mS = W.mS;
+    a.dg = W.dg;
+    a.w = W.w;
+    a.rcomp = W.rcomp;
+    a.uh = W.uh.p;
+    a.ul = W.ul.p;
+    a.rh = W.rh.p;
+    a.rl = W.rl.p;
+    a.dv[0] = reinterpret_cast<float4*>(W.d0.p);
+    a.dv[1] = reinterpret_cast<float4*>(W.d1.p);
+    a.ri = reinterpret_cast<float4*>(W.ri.p);
+    a.z = reinterpret_cast<float4*>(W.z.p);
+    a.p = reinterpret_cast<float4*>(W.p.p);
+    a.q = reinterpret_cast<float4*>(W.q.p);
+    a.partials = W.partials;
+    a.fin = W.fin;
+    a.sigpart = W.sigpart;
+    a.bar = W.bar;
+    a.status = W.status;
+    a.fnew = W.fnew;
+    a.fold = W.fold;
+    a.qv = W.qv;
+    a.gv = W.gv;
+    a.seqv = W.seqv;
+    a.n_steps = n_steps;
+    a.sched_stride = S.n_steps;
+    BT_REQUIRE(n_steps >= 1 && n_steps <= S.n_steps, BT_ERR_INVALID, "mixed stepper: bad step count");
+    a.maxit = maxit;
+    a.max_sweeps = ctx->opt_mixed_max_sweeps;
+    a.theta = (float)S.theta;
+    a.inv_k = (float)(1.0 / S.dt);
+    a.rtol = (float)rtol;
+    a.eps_first = (float)ctx->opt_mixed_eps_first;
+    a.eps_next = (float)ctx->opt_mixed_eps_next;
+    a.two_stage = ((size_t)nb * Rp * kNV > 16384) ? 1 : 0;
+    a.iters = W.iters;
+    a.sweeps = W.sweeps;
+    a.sig = W.sig;
+    a.diag = W.diag;
+    {
+        const void* need_ptrs[] = {a.row_ptr, a.col, a.mA, a.mL, a.mS, a.dg, a.w, a.rcomp, a.uh, a.ul, a.rh, a.rl,
+                                   a.dv[0], a.dv[1], a.ri, a.z, a.p, a.q, a.partials, a.fin, a.sigpart, a.bar,
+                                   a.status, a.fnew, a.fold, a.qv, a.gv, a.seqv, a.iters, a.sweeps, a.sig, a.diag};
+        for (const void* ptr : need_ptrs)
+            BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "mixed stepper: a device buffer is not allocated");
+    }
+    void* args[] = {&a};
+    BT_CUDA(cudaEventRecord(ctx->ev1, s));
+    BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(nb), dim3(kThreadsB), args, 0, s));
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    int hst = 0;
+    float hdiag[8];
+    BT_CUDA(cudaMemcpyAsync(&hst, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BT_CUDA(cudaMemcpyAsync(hdiag, W.diag.p, sizeof(hdiag), cudaMemcpyDeviceToHost, s));
+    BT_CUDA(cudaStreamSynchronize(s));
+    if (hst == DEV_NOT_CONVERGED) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "mixed stepper: %s did not converge (step %d, sweep %d, iteration %d, RHS %d at %.3g x its "
+                 "target; lanes-per-row %d, %d blocks)",
+                 hdiag[0] == 1.0f ? "inner COCG" : "the refinement", (int)hdiag[1], (int)hdiag[2], (int)hdiag[3],
+                 (int)hdiag[5], hdiag[4], lpr, nb);
+        throw Error(BT_ERR_NOT_CONVERGED, msg);
+    }
+    map_status_mixed(hst);
+    float ms = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
+    W.Rp = Rp;
+    W.nb = nb;
+    return ms;
+}
+
+// Measuring autotuner: for this (n, R) try every valid lanes-per-row with 1 and
+// the maximum co-resident blocks per SM on a 3-step run, keep the fastest.
+static std::pair<int, int> autotune_mixed(bt_ctx* ctx, SolverMixed& W, int R, double rtol, int maxit,
+                                          const double* d_u0) {
+    if (ctx->opt_mixed_lpr > 0)
+        return {ctx->opt_mixed_lpr, ctx->opt_mixed_blocks_per_sm > 0 ? ctx->opt_mixed_blocks_per_sm : 2};
+    const auto key = std::make_pair(ctx->mesh.n_dofs, R);
+    auto it = W.tuned.find(key);
+    if (it != W.tuned.end()) return it->second;
+    std::pair<int, int> best{-1, 1};
+    float best_ms = 1e30f;
+    const int steps = std::min(3, ctx->sched.n_steps);
+    for (int lpr : lpr_candidates(R)) {
+        for (int bps : {1, 2, 4}) {
+            const float ms = launch_batch(ctx, W, R, lpr, bps, steps, rtol, maxit, d_u0);
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = {lpr, bps};
+            }
+        }
+    }
+    BT_REQUIRE(best.first > 0, BT_ERR_INVALID, "mixed stepper: no valid geometry for this batch size");
+    W.tuned[key] = best;
+    return best;
+}
+
+void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
+                 const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st) {
+    Mesh& m = ctx->mesh;
+    Assembled& A = ctx->mat;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    if (!ctx->smx) ctx->smx = new SolverMixed();
+    SolverMixed& W = *ctx->smx;
+    const int64_t nnz = m.nnz;
+    W.mA.alloc(nnz);
+    W.mL.alloc(nnz);
+    W.mS.alloc(nnz);
+    W.dg.alloc(m.n_dofs);
+    W.w.alloc(m.n_dofs);
+    W.rcomp.alloc(m.n_dofs);
+    W.iters.alloc(S.n_steps);
+    W.sweeps.alloc(S.n_steps);
+    k_pack_mixed<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz,
+                                                              1.0 / S.dt, S.theta, W.mA, W.mL, W.mS);
+    BT_CUDA(cudaGetLastError());
+    W.fnew.upload(S.f_new.data(), S.f_new.size(), s);
+    W.fold.upload(S.f_old.data(), S.f_old.size(), s);
+    if (u0) W.u0.upload(u0, m.n_v, s);
+    const double* d_u0 = u0 ? W.u0.p : nullptr;
+    if (st) {
+        st->steps = S.n_steps;
+        st->max_iterations = 0;
+        st->total_iterations = 0;
+        st->max_rel_residual = rtol;
+        st->refinements = 0;
+        st->graph_launches = 0;
+        st->kernel_launches = 0;
+        st->stepper_ms = 0.0;
+    }
+    ctx->last_iters.assign((size_t)nsig * S.n_steps, 0);
+    // final states are kept for bt_get_solution only for modest batches (the
+    // copy is n_dofs x n_signals complex values through the host)
+    const bool keep = (int64_t)nsig * m.n_dofs <= (int64_t)8 * 1024 * 1024;
+    W.saved.assign(keep ? (size_t)nsig * m.n_dofs : 0, make_double2(0.0, 0.0));
+    W.saved_nsig = keep ? nsig : 0;
+    BT_CUDA(cudaEventRecord(ctx->ev0, s));
+    float stepper_ms = 0.0f;
+    std::vector<int32_t> hit(S.n_steps), hsw(S.n_steps);
+    for (int32_t b0 = 0; b0 < nsig; b0 += kMaxRhs / 2) {
+        const int NS = std::min<int32_t>(kMaxRhs / 2, nsig - b0);   // signals in this launch
+        const int R = 2 * NS;                                        // slots: Re and Im of each
+        // per-RHS parameters for all kMaxRhs slots, padded with copies of the last
+        // real RHS (padding slots start from u = 0 and never iterate)
+        const int Rmax = kMaxRhs;
+        std::vector<double> hq(Rmax);
+        std::vector<float> hg(Rmax * 3);
+        std::vector<int32_t> hs(Rmax);
+        for (int r = 0; r < Rmax; ++r) {
+            const int src = b0 + std::min(r / 2, NS - 1);
+            hq[r] = q[src];
+            for (int k = 0; k < 3; ++k) hg[r * 3 + k] = (float)gdir[3 * src + k];
+            hs[r] = seq ? seq[src] : 0;
+            BT_REQUIRE(hs[r] >= 0 && hs[r] < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
+        }
+        W.qv.upload(hq.data(), Rmax, s);
+        W.gv.upload(hg.data(), (size_t)Rmax * 3, s);
+        W.seqv.upload(hs.data(), Rmax, s);
+        const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, d_u0);
+        const float ms = launch_batch(ctx, W, R, geo.first, geo.second, S.n_steps, rtol, maxit, d_u0);
+        stepper_ms += ms;
+        const int Rp = W.Rp;
+        std::vector<double> hsig((size_t)Rp * (1 + kMaxCompartments));
+        W.sig.download(hsig.data(), hsig.size(), s);
+        W.iters.download(hit.data(), S.n_steps, s);
+        W.sweeps.download(hsw.data(), S.n_steps, s);
+        // final solutions (hi + lo) for bt_get_solution
+        const int nsr = Rp / 2;   // signals per row in the per-signal arrays
+        std::vector<float2> huh(keep ? (size_t)m.n_dofs * nsr : 0), hul(keep ? (size_t)m.n_dofs * nsr : 0);
+        if (keep) {
+            W.uh.download(huh.data(), huh.size(), s);
+            W.ul.download(hul.data(), hul.size(), s);
+        }
+        BT_CUDA(cudaStreamSynchronize(s));
+        for (int r = 0; r < NS; ++r) {
+            const size_t so = (size_t)(2 * r) * (1 + kMaxCompartments);   // signal r lives in slot 2r
+            sig[b0 + r] = hsig[so];
+            if (comp_sig)
+                for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)(b0 + r) * m.n_comp + c] = hsig[so + 1 + c];
+            for (int64_t i = 0; keep && i < m.n_dofs; ++i) {
+                const float2 h = huh[(size_t)i * nsr + r], l = hul[(size_t)i * nsr + r];
+                W.saved[(size_t)(b0 + r) * m.n_dofs + i] = make_double2((double)h.x + l.x, (double)h.y + l.y);
+            }
+            for (int k = 0; k < S.n_steps; ++k) ctx->last_iters[(size_t)(b0 + r) * S.n_steps + k] = hit[k];
+        }
+        if (st) {
+            for (int k = 0; k < S.n_steps; ++k) {
+                st->max_iterations = std::max(st->max_iterations, hit[k]);
+                st->total_iterations += (int64_t)hit[k] * NS;
+                st->refinements += hsw[k];
+            }
+            st->kernel_launches += 3;
+        }
+    }
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    BT_CUDA(cudaEventSynchronize(ctx->ev2));
+    float total = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&total, ctx->ev0, ctx->ev2));
+    if (st) {
+        st->gpu_ms = total;
+        st->stepper_ms = stepper_ms;
+    }
+    ctx->last_nsig = nsig;
+}
+
+void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u) {
+    BT_REQUIRE(ctx->smx && index >= 0 && index < ctx->smx->saved_nsig, BT_ERR_INVALID,
+               "bt_get_solution: no such signal in the last mixed solve (states of batches above "
+               "8M dof-signals are not kept)");
+    const int64_t n = ctx->mesh.n_dofs;
+    const double2* src = ctx->smx->saved.data() + (size_t)index * n;
+    for (int64_t i = 0; i < n; ++i) {
+        u[2 * i] = src[i].x;
+        u[2 * i + 1] = src[i].y;
+    }
+}
+
 void free_solver_mixed(bt_ctx* ctx) {
     delete ctx->smx;
     ctx->smx = nullptr;

@@ -165,6 +165,13 @@ struct bt_ctx {
     int32_t last_precision = -1;
     std::vector<int32_t> last_iters;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    // tuning knobs (bt_set_option); negative = automatic
+    int opt_mixed_lpr = -1;
+    int opt_mixed_blocks_per_sm = -1;
+    int opt_mixed_max_sweeps = 8;
+    double opt_mixed_eps_first = 1e-4;
+    double opt_mixed_eps_next = 3e-3;
+    int opt_fp64_extrapolate = 1;
 };
 
 namespace bt {

@@ -17,12 +17,19 @@
 // Vectors are double2 (re, im) of length n_pad = 32 * slices.
 //
 // One kernel runs all steps and iterations; phases are separated by a bounded
-// grid barrier (bt_common.cuh).  Two barriers per COCG iteration: the search
-// direction update p = z + beta p is folded into the SpMV (each row forms
-// z_j + beta p_j of its neighbours on the fly and the owner writes its own p
-// to a second buffer), so the iteration is
-//   phase A:  p' = z + beta p,  q = A p',  mu = p'^T q           | barrier
-//   phase B:  x += alpha p', r -= alpha q, z = D^-1 r, rho = r^T z | barrier
+// grid barrier (bt_common.cuh).  GB300 executes FP64 at a small fraction of
+// its FP32 rate, so the loop is arranged to minimise FP64 operations:
+//   * q = A p is carried by the recurrence q = A z + beta q (p = z + beta p),
+//     so the only SpMV of an iteration is A z: 4 FP64 FMAs per stored entry;
+//   * the Jacobi inverse D^-1 = 1 / (A_re,ii + i cn J_ii) is formed once per
+//     step (phase R), not per iteration;
+//   * the initial guess is the linear extrapolation 2 u_n - u_{n-1}, which
+//     saves iterations at the cost of one extra gather in phase R.
+// Per iteration (two barriers):
+//   phase A:  w = A z ; q = w + beta q ; p = z + beta p ; mu = p^T q   | barrier
+//   phase B:  x += alpha p ; r -= alpha q ; z = D^-1 r ; rho = r^T z  | barrier
+// The three solution levels u_{n-1}, u_n, u_{n+1} rotate through three
+// buffers so that phase R can gather u_{n-1} and u_n while writing u_{n+1}.
 // Reductions are per-block partials summed by every block in block order, so
 // all blocks take identical decisions and results are bitwise reproducible.
 #include "bt_common.cuh"
@@ -42,7 +49,7 @@ struct Solver64 {
     DevBuf<double> bre;          // SELL B_re
     DevBuf<double> dA, dJ, w;    // per row
     DevBuf<int32_t> rcomp;       // compartment per row (-1 padding)
-    DevBuf<double2> x, r, z, pa, pb, q;
+    DevBuf<double2> u[3], r, z, p, q, dinv;
     DevBuf<double> partials;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
@@ -64,12 +71,14 @@ struct StepArgs {
     const double* __restrict__ dJ;
     const double* __restrict__ w;
     const int32_t* __restrict__ rcomp;
-    double2* x;
+    double2* u0;
+    double2* u1;
+    double2* u2;
     double2* r;
     double2* z;
-    double2* pa;
-    double2* pb;
+    double2* p;
     double2* q;
+    double2* dinv;
     double* partials;
     unsigned* bar;
     int* status;
@@ -78,6 +87,7 @@ struct StepArgs {
     int32_t n_steps;
     int32_t maxit;
     int32_t nc;
+    int32_t extrapolate;
     double rtol2;
     int32_t* iters;
     double* relres;
@@ -132,31 +142,49 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
     const int total_warps = gridDim.x * warps_per_block;
     const unsigned nb = gridDim.x;
     unsigned gen = 0, flip = 0;
+    double2* U[3] = {a.u0, a.u1, a.u2};
+    double2* x = U[1];
 
     for (int step = 0; step < a.n_steps; ++step) {
         const double cn = a.cn[step], co = a.co[step];
-        // ---- phase R: b = (B_re - i co J) x ; r = b - (A_re + i cn J) x ; z = D^-1 r
+        const double2* __restrict__ cur = U[step % 3];
+        const double2* __restrict__ prev = U[(step + 2) % 3];
+        x = U[(step + 1) % 3];
+        // ---- phase R: b = (B_re - i co J) u_n ; x = 2 u_n - u_{n-1} ;
+        //               r = b - A x ; D^-1 ; z = D^-1 r
         double acc[4] = {0.0, 0.0, 0.0, 0.0};  // rho.re, rho.im, |r|^2, |b|^2
         for (int s = gw; s < a.n_slices; s += total_warps) {
             const int32_t base = a.sl_ptr[s], wdt = a.sl_w[s];
-            double2 sA = make_double2(0.0, 0.0), sJ = sA, sB = sA;
+            double2 sA = make_double2(0.0, 0.0), sJ = sA, sB = sA, tA = sA, tJ = sA;
             for (int k = 0; k < wdt; ++k) {
                 const int32_t e = base + k * 32 + lane;
                 const int32_t c = a.col[e];
                 const double2 m = a.aj[e];
                 const double br = a.bre[e];
-                const double2 xj = a.x[c];
-                sA.x = fma(m.x, xj.x, sA.x); sA.y = fma(m.x, xj.y, sA.y);
-                sJ.x = fma(m.y, xj.x, sJ.x); sJ.y = fma(m.y, xj.y, sJ.y);
-                sB.x = fma(br, xj.x, sB.x);  sB.y = fma(br, xj.y, sB.y);
+                const double2 uj = cur[c], vj = prev[c];
+                sA.x = fma(m.x, uj.x, sA.x); sA.y = fma(m.x, uj.y, sA.y);
+                sJ.x = fma(m.y, uj.x, sJ.x); sJ.y = fma(m.y, uj.y, sJ.y);
+                sB.x = fma(br, uj.x, sB.x);  sB.y = fma(br, uj.y, sB.y);
+                tA.x = fma(m.x, vj.x, tA.x); tA.y = fma(m.x, vj.y, tA.y);
+                tJ.x = fma(m.y, vj.x, tJ.x); tJ.y = fma(m.y, vj.y, tJ.y);
             }
             const int64_t i = (int64_t)s * 32 + lane;
             const double2 b = make_double2(fma(co, sJ.y, sB.x), fma(-co, sJ.x, sB.y));
-            const double2 ax = make_double2(fma(-cn, sJ.y, sA.x), fma(cn, sJ.x, sA.y));
+            // A x0 with x0 = 2 u_n - u_{n-1} (or u_n)
+            const double ex = a.extrapolate ? 1.0 : 0.0;
+            const double2 gA = make_double2(sA.x + ex * (sA.x - tA.x), sA.y + ex * (sA.y - tA.y));
+            const double2 gJ = make_double2(sJ.x + ex * (sJ.x - tJ.x), sJ.y + ex * (sJ.y - tJ.y));
+            const double2 ax = make_double2(fma(-cn, gJ.y, gA.x), fma(cn, gJ.x, gA.y));
+            const double2 ui = cur[i], vi = prev[i];
+            x[i] = make_double2(ui.x + ex * (ui.x - vi.x), ui.y + ex * (ui.y - vi.y));
             const double2 rr = make_double2(b.x - ax.x, b.y - ax.y);
-            const double2 zz = cmul(cinv(make_double2(a.dA[i], cn * a.dJ[i])), rr);
+            const double2 di = cinv(make_double2(a.dA[i], cn * a.dJ[i]));
+            const double2 zz = cmul(di, rr);
+            a.dinv[i] = di;
             a.r[i] = rr;
             a.z[i] = zz;
+            a.p[i] = make_double2(0.0, 0.0);
+            a.q[i] = make_double2(0.0, 0.0);
             const double2 rz = cmul(rr, zz);
             acc[0] += rz.x;
             acc[1] += rz.y;
@@ -169,8 +197,6 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
         const double bb2 = acc[3];
         const double tol2 = a.rtol2 * bb2;
         double2 beta = make_double2(0.0, 0.0);
-        double2* pold = a.pa;
-        double2* pnew = a.pb;
         int it = 0;
         bool failed = false;  // uniform across the grid: every block sees the same sums
         while (rr2 > tol2) {
@@ -179,7 +205,7 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 failed = true;
                 break;
             }
-            // ---- phase A: p' = z + beta p ; q = A p' ; mu = p'^T q
+            // ---- phase A: w = A z ; q = w + beta q ; p = z + beta p ; mu = p^T q
             double mu[2] = {0.0, 0.0};
             for (int s = gw; s < a.n_slices; s += total_warps) {
                 const int32_t base = a.sl_ptr[s], wdt = a.sl_w[s];
@@ -188,20 +214,18 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                     const int32_t e = base + k * 32 + lane;
                     const int32_t c = a.col[e];
                     const double2 m = a.aj[e];
-                    const double2 zc = a.z[c], pc = pold[c];
-                    const double2 pj = make_double2(zc.x + (beta.x * pc.x - beta.y * pc.y),
-                                                    zc.y + (beta.x * pc.y + beta.y * pc.x));
-                    sA.x = fma(m.x, pj.x, sA.x); sA.y = fma(m.x, pj.y, sA.y);
-                    sJ.x = fma(m.y, pj.x, sJ.x); sJ.y = fma(m.y, pj.y, sJ.y);
+                    const double2 zc = a.z[c];
+                    sA.x = fma(m.x, zc.x, sA.x); sA.y = fma(m.x, zc.y, sA.y);
+                    sJ.x = fma(m.y, zc.x, sJ.x); sJ.y = fma(m.y, zc.y, sJ.y);
                 }
                 const int64_t i = (int64_t)s * 32 + lane;
-                const double2 zi = a.z[i], pi = pold[i];
-                const double2 pn = make_double2(zi.x + (beta.x * pi.x - beta.y * pi.y),
-                                                zi.y + (beta.x * pi.y + beta.y * pi.x));
-                const double2 qi = make_double2(fma(-cn, sJ.y, sA.x), fma(cn, sJ.x, sA.y));
-                pnew[i] = pn;
-                a.q[i] = qi;
-                const double2 pq = cmul(pn, qi);
+                const double2 zi = a.z[i], pi = a.p[i], qo = a.q[i];
+                const double2 bp = cmul(beta, pi), bq = cmul(beta, qo);
+                const double2 pn = make_double2(zi.x + bp.x, zi.y + bp.y);
+                const double2 qn = make_double2(fma(-cn, sJ.y, sA.x) + bq.x, fma(cn, sJ.x, sA.y) + bq.y);
+                a.p[i] = pn;
+                a.q[i] = qn;
+                const double2 pq = cmul(pn, qn);
                 mu[0] += pq.x;
                 mu[1] += pq.y;
             }
@@ -214,17 +238,17 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 break;
             }
             const double2 alpha = cdiv(rho, muv);
-            // ---- phase B: x += alpha p' ; r -= alpha q ; z = D^-1 r
+            // ---- phase B: x += alpha p ; r -= alpha q ; z = D^-1 r
             double acc3[3] = {0.0, 0.0, 0.0};
             for (int s = gw; s < a.n_slices; s += total_warps) {
                 const int64_t i = (int64_t)s * 32 + lane;
-                const double2 pn = pnew[i], qi = a.q[i];
-                double2 xi = a.x[i], ri = a.r[i];
+                const double2 pn = a.p[i], qi = a.q[i];
+                double2 xi = x[i], ri = a.r[i];
                 const double2 ap = cmul(alpha, pn), aq = cmul(alpha, qi);
                 xi.x += ap.x; xi.y += ap.y;
                 ri.x -= aq.x; ri.y -= aq.y;
-                const double2 zi = cmul(cinv(make_double2(a.dA[i], cn * a.dJ[i])), ri);
-                a.x[i] = xi;
+                const double2 zi = cmul(a.dinv[i], ri);
+                x[i] = xi;
                 a.r[i] = ri;
                 a.z[i] = zi;
                 const double2 rz = cmul(ri, zi);
@@ -246,9 +270,6 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
             }
             beta = cdiv(rho_new, rho);
             rho = rho_new;
-            double2* t = pold;
-            pold = pnew;
-            pnew = t;
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             a.iters[step] = it;
@@ -256,9 +277,9 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
         }
         if (failed) return;
         // The last phase B (or phase R when no iteration ran) ended in a grid
-        // barrier, so every x written this step is visible to the next phase R.
+        // barrier, so u_{n+1} is complete before the next phase R gathers it.
     }
-    // ---- signal: S = sum w Re(x), per compartment
+    // ---- signal: S = sum w Re(u_N), per compartment
     double acc[kRed];
 #pragma unroll
     for (int k = 0; k < kRed; ++k) acc[k] = 0.0;
@@ -266,7 +287,7 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
         const int64_t i = (int64_t)s * 32 + lane;
         const int c = a.rcomp[i];
         if (c >= 0) {
-            const double v = a.w[i] * a.x[i].x;
+            const double v = a.w[i] * x[i].x;
             acc[0] += v;
 #pragma unroll
             for (int k = 0; k < kMaxCompartments; ++k)
@@ -305,8 +326,8 @@ __global__ void k_rows64(int64_t n, int64_t n_pad, const int32_t* __restrict__ d
                          const double* __restrict__ wsrc, const int32_t* __restrict__ comp,
                          const int32_t* __restrict__ dof_vertex, const double* __restrict__ u0,
                          double* __restrict__ dA, double* __restrict__ dJ, double* __restrict__ w,
-                         int32_t* __restrict__ rcomp, double2* __restrict__ x, double2* __restrict__ pa,
-                         double2* __restrict__ pb) {
+                         int32_t* __restrict__ rcomp, double2* __restrict__ x, double2* __restrict__ xprev,
+                         double2* __restrict__ pa) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_pad) return;
     if (i < n) {
@@ -316,15 +337,16 @@ __global__ void k_rows64(int64_t n, int64_t n_pad, const int32_t* __restrict__ d
         w[i] = wsrc[i];
         rcomp[i] = comp[i];
         x[i] = make_double2(u0 ? u0[dof_vertex[i]] : 1.0, 0.0);
+        xprev[i] = x[i];
     } else {
         dA[i] = 1.0;
         dJ[i] = 0.0;
         w[i] = 0.0;
         rcomp[i] = -1;
         x[i] = make_double2(0.0, 0.0);
+        xprev[i] = x[i];
     }
     pa[i] = make_double2(0.0, 0.0);
-    pb[i] = make_double2(0.0, 0.0);
 }
 
 static void map_status(int st) {
@@ -352,7 +374,7 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
     W.bre.alloc(W.sell);
     W.dA.alloc(W.n_pad); W.dJ.alloc(W.n_pad); W.w.alloc(W.n_pad);
     W.rcomp.alloc(W.n_pad);
-    for (auto* v : {&W.x, &W.r, &W.z, &W.pa, &W.pb, &W.q}) v->alloc(W.n_pad);
+    for (auto* v : {&W.u[0], &W.u[1], &W.u[2], &W.r, &W.z, &W.p, &W.q, &W.dinv}) v->alloc(W.n_pad);
     W.bar.alloc(2);
     W.status.alloc(1);
     W.cn.alloc(S.n_steps); W.co.alloc(S.n_steps);
@@ -405,7 +427,7 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
                                                                  A.Jy, A.Jz, W.gq, inv_k, S.theta, W.aj, W.bre);
         k_rows64<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(
             n, W.n_pad, m.diag_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz, W.gq, inv_k, S.theta, A.w, m.dof_comp,
-            m.dof_vertex, u0 ? d_u0.p : nullptr, W.dA, W.dJ, W.w, W.rcomp, W.x, W.pa, W.pb);
+            m.dof_vertex, u0 ? d_u0.p : nullptr, W.dA, W.dJ, W.w, W.rcomp, W.u[0], W.u[2], W.u[1]);
         BT_CUDA(cudaGetLastError());
         W.bar.zero(s);
         W.status.zero(s);
@@ -413,20 +435,29 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
         a.n_slices = m.n_slices;
         a.sl_ptr = m.sl_ptr; a.sl_w = m.sl_w; a.col = m.sl_col;
         a.aj = W.aj; a.bre = W.bre; a.dA = W.dA; a.dJ = W.dJ; a.w = W.w; a.rcomp = W.rcomp;
-        a.x = W.x; a.r = W.r; a.z = W.z; a.pa = W.pa; a.pb = W.pb; a.q = W.q;
+        a.u0 = W.u[0]; a.u1 = W.u[1]; a.u2 = W.u[2];
+        a.r = W.r; a.z = W.z; a.p = W.p; a.q = W.q; a.dinv = W.dinv;
         a.partials = W.partials; a.bar = W.bar; a.status = W.status;
         a.cn = W.cn; a.co = W.co;
         a.n_steps = S.n_steps;
         a.maxit = maxit;
         a.nc = m.n_comp;
+        a.extrapolate = ctx->opt_fp64_extrapolate;
         a.rtol2 = rtol * rtol;
         a.iters = W.iters; a.relres = W.relres; a.out = W.out;
+        {
+            const void* need_ptrs[] = {a.sl_ptr, a.sl_w, a.col, a.aj, a.bre, a.dA, a.dJ, a.w, a.rcomp, a.u0, a.u1,
+                                       a.u2, a.r, a.z, a.p, a.q, a.dinv, a.partials, a.bar, a.status, a.cn, a.co,
+                                       a.iters, a.relres, a.out};
+            for (const void* ptr : need_ptrs)
+                BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "stepper: a device buffer is not allocated");
+        }
         void* args[] = {&a};
         BT_CUDA(cudaEventRecord(ctx->ev1, s));
         BT_CUDA(cudaLaunchCooperativeKernel((const void*)k_step64, dim3(W.nblocks), dim3(kThreads64), args, 0, s));
         BT_CUDA(cudaEventRecord(ctx->ev2, s));
-        BT_CUDA(cudaMemcpyAsync(W.saved.p + (size_t)sg * W.n_pad, W.x.p, W.n_pad * sizeof(double2),
-                                cudaMemcpyDeviceToDevice, s));
+        BT_CUDA(cudaMemcpyAsync(W.saved.p + (size_t)sg * W.n_pad, W.u[S.n_steps % 3].p,
+                                W.n_pad * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         int hst = 0;
         BT_CUDA(cudaMemcpyAsync(&hst, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
         W.out.download(hout.data(), kRed, s);

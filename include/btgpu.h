@@ -150,6 +150,15 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
              double rtol, int32_t max_iterations, double* signal_out,
              double* compartment_out, double* S0_out, bt_stats* stats);
 
+/* Tuning knobs (no counterpart in the reference).  Keys:
+ *   "mixed.lanes_per_row"   1,2,4,...,32 (0: autotune, the default)
+ *   "mixed.blocks_per_sm"   co-resident blocks of the batched kernel (0: autotune)
+ *   "mixed.max_sweeps"      refinement sweeps per step (default 8)
+ *   "mixed.eps_first"       inner FP32 tolerance of the first sweep (1e-4)
+ *   "mixed.eps_next"        inner FP32 tolerance of later sweeps (3e-3)
+ *   "fp64.extrapolate"      1: initial guess 2 u_n - u_{n-1} (default), 0: u_n */
+int bt_set_option(bt_ctx* ctx, const char* key, double value);
+
 /* Introspection for tests (no counterpart in the reference). */
 int bt_get_csr(bt_ctx* ctx, int32_t* row_ptr /* n_dofs+1 */, int32_t* col /* nnz */);
 int bt_get_matrix(bt_ctx* ctx, int32_t which, double* values /* nnz */);
