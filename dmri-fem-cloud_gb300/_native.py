@@ -32,6 +32,7 @@ EXPORTS = [
     "bt_mesh_upload", "bt_mesh_info", "bt_set_coefficients", "bt_set_cell_diffusion",
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
+    "bt_signal_noalloc",
 ]
 
 
@@ -99,6 +100,7 @@ def load(path=None):
         "bt_get_solution": (C.c_int, [_P, C.c_int32, _D]),
         "bt_get_iterations": (C.c_int, [_P, _I32, C.c_int64]),
         "bt_set_option": (C.c_int, [_P, C.c_char_p, C.c_double]),
+        "bt_signal_noalloc": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -159,6 +159,22 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
  *   "fp64.extrapolate"      1: initial guess 2 u_n - u_{n-1} (default), 0: u_n */
 int bt_set_option(bt_ctx* ctx, const char* key, double value);
 
+/* Signal functional S = sum_i weights[i] * Re(u[i]) of a device-resident state,
+ * computed without allocating any memory.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc when they read a signal (code running
+ * inside CUDA stream capture, a serving or acquisition thread whose allocator is
+ * frozen after start-up).  d_weights[n] are the per-dof signal weights
+ * (bt_get_dofs), d_u[2n] the state as (re, im) pairs (bt_get_solution layout),
+ * d_signal one double; all are device pointers.  Work is enqueued on
+ * cuda_stream (NULL: the legacy default stream) of the current device.
+ * Scratch is a static 8 KB device array: n <= 2097152, larger n returns
+ * BT_ERR_INVALID.  The first call on each device looks up that array's device
+ * address, so make it before any stream capture begins.  Calls share the
+ * scratch: calls that overlap on the GPU race and must be serialised.
+ * Returns a status code only (no context, so no bt_last_error text). */
+int bt_signal_noalloc(const double* d_weights, const double* d_u, int64_t n, double* d_signal,
+                      void* cuda_stream);
+
 /* Introspection for tests (no counterpart in the reference). */
 int bt_get_csr(bt_ctx* ctx, int32_t* row_ptr /* n_dofs+1 */, int32_t* col /* nnz */);
 int bt_get_matrix(bt_ctx* ctx, int32_t which, double* values /* nnz */);
