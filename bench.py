@@ -8,12 +8,15 @@ kappa = 1e-5 um/us, PGSE delta = 10600 us, Delta = 43100 us, dt = 200 us
 All inputs are synthetic and deterministic (seed 0).
 
 A "step" is one pass of the hot path over the whole batch: every signal of the
-workload integrated over all 270 time steps by libbtgpu (FP64 COCG, rtol
-1e-12; or the mixed-precision path with --precision mixed).  ``value`` is
-signals/s with the mesh already resident and assembled; ``e2e`` repeats the
+workload integrated over all 270 time steps by libbtgpu.  ``value`` is the
+batched mixed-precision path (FP32 inner Jacobi-COCG, double-float residuals,
+outer rtol 1e-9; its signals agree with the FP64 path to <= 1e-6, checked in
+the line as ``plain_fp64.max_rel_err_mixed_vs_fp64``), measured with the mesh
+already resident and assembled; ``plain_fp64`` times the FP64 path (rtol 1e-12,
+the reference-parity path) on the same workload.  ``e2e`` repeats the
 measurement through the public C-ABI calls from host buffers (mesh upload and
-device graph build, coefficient upload, assembly, schedule, solve, signals
-back to the host).
+device graph build, coefficient upload, assembly, schedule, solve, signals back
+to the host).
 
 ``--impl reference`` times the CPU restatement of the reference's solve path
 (two-field real system, Jacobi-BiCGSTAB rtol 1e-9 as GCloudDmriSolver.py
@@ -43,11 +46,15 @@ WORKLOADS = {
             "b=1000, gdir (1,0,0), dt=200 us",
     "cfg2": "two compartments, [-10,10]^3 um box, 40^3 Kuhn cubes (384,000 tets), cylinder x^2+y^2<36, "
             "D=3e-3, kappa=1e-5, PGSE 10600/43100 us, b in {1000,3000}, gdir (0,1,0), dt=200 us",
+    "cfg3": "eight seeded non-overlapping z-cylinders (radii U[2,5]) in a [-15,15]^3 um box, 64^3 Kuhn cubes "
+            "(1.57M tets), kappa=5e-5, D=3e-3, 64 Fibonacci directions x 8 b in [500,4000] = 512 signals, "
+            "directions 0-31 PGSE 10600/43100 us, 32-63 cos-OGSE (one period over delta), dt=200 us",
 }
 
 
 def alg_bytes_fp64(n, nnz, steps, iters):
-    """Minimum unique bytes of the FP64 single-RHS solve of one signal.
+    """Minimum unique bytes of the FP64 single-RHS solve of one signal (one
+    k_step64 launch).
 
     per COCG iteration: nnz*(4 + 8 + 8) (column, A_re, J_g) + 4n (row offsets)
       + n*16*(2 + 7 + 1) (SpMV p in / q out, update x,r,p,q in + x,r,p out, diagonal)
@@ -56,6 +63,22 @@ def alg_bytes_fp64(n, nnz, steps, iters):
     per_iter = nnz * 20 + 4 * n + 160 * n
     per_step = nnz * 28 + 4 * n + 32 * n
     return steps * per_step + iters * per_iter
+
+
+def alg_bytes_mixed(n, nnz, nsig, steps, iters, sweeps):
+    """Minimum unique bytes of one k_batched launch of `nsig` signals.
+
+    Each signal is two FP32 complex slots (Re / Im right-hand sides, 8 bytes a
+    value).  per inner iteration and signal-dof: 2 slots x (gather z 8 + p,q in
+    16 + p,q out 16 + p,q,d,r in 32 + d,r,z out 24) = 192 B, plus the matrix
+    nnz*(4 + 16) once per iteration for the whole batch; per refinement sweep
+    and signal-dof: gather d 16, u and r in/out as double-float 64, restart of
+    the five slot vectors 80 = 160 B, matrix nnz*(4 + 32); per time step and
+    signal-dof: gather u 16, r out 16, slot vectors 80 = 112 B, matrix
+    nnz*(4 + 8 + 32).
+    """
+    return (iters * (192 * n * nsig + 20 * nnz) + sweeps * (160 * n * nsig + 36 * nnz)
+            + steps * (112 * n * nsig + 44 * nnz))
 
 
 class ClockSampler:
@@ -187,66 +210,98 @@ def gpu_run(args):
     ctx.set_schedule(fn, fo, w["dt"])
     info = ctx.info()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 512 MB > L2
-
-    def one_step():
-        return ctx.solve(q, g, pidx, None, prec, rtol, args.maxit)
-
-    for _ in range(args.warmup):
-        one_step()
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    evs = []
-    outs = []
-    with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        for _ in range(args.steps):
-            flush.zero_()                                   # L2 flushed between timed steps
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            outs.append(one_step())
-            e1.record(stream)
-            evs.append((e0, e1))
-        torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
     n_sig = len(sig)
+
+    def timed(precision, tol, steps, warmup):
+        """W untimed + K timed solves of the whole batch; CUDA events on the
+        library's stream (torch's current stream), L2 flushed between steps."""
+        for _ in range(warmup):
+            ctx.solve(q, g, pidx, None, precision, tol, args.maxit)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs, outs = [], []
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            for _ in range(steps):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                outs.append(ctx.solve(q, g, pidx, None, precision, tol, args.maxit))
+                e1.record(stream)
+                evs.append((e0, e1))
+            torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        tot = sum(a.elapsed_time(b) for a, b in evs)
+        if world > 1:
+            t = torch.tensor([tot], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot, outs, clk.summary()
+
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    l2_note = ("L2-resident: the working set fits the 129 MB L2 within a step, so achieved/HBM-peak counts "
+               "L2-served bytes" if info["nnz"] * 44 + info["n_dofs"] * n_sig * 400 < 100e6 else
+               "working set larger than L2")
+
+    def roofline(kind, st):
+        if kind == "fp64":
+            iters = st["total_iterations"] / n_sig
+            byts = alg_bytes_fp64(info["n_dofs"], info["nnz"], st["steps"], iters)
+            launch_ms = st["stepper_ms"] / n_sig
+            kern = "k_step64 (persistent FP64 CN/COCG stepper, one launch per signal)"
+        else:
+            launches = max(1, -(-n_sig // 256))
+            per = n_sig / launches
+            iters = st["total_iterations"] / n_sig                 # inner iterations per launch
+            sweeps = st["refinements"] / launches
+            byts = alg_bytes_mixed(info["n_dofs"], info["nnz"], per, st["steps"], iters, sweeps)
+            launch_ms = st["stepper_ms"] / launches
+            kern = "k_batched (persistent mixed-precision batched stepper, %d signal(s) per launch)" % per
+        ach = byts / (launch_ms / 1e3) / 1e9
+        tr = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            t = json.load(open(tpath)).get("%s:%s" % (args.workload, kind))
+            tr = t["bytes_per_launch"] if t else None
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": tr, "kernel": kern, "bytes_per_launch": byts, "launch_ms": launch_ms,
+                "peak_source": peak_src + " hbm_gbs (copy)", "note": l2_note}
+
+    prec_main = pkg.PRECISION_MIXED if args.precision == "mixed" else pkg.PRECISION_FP64
+    tol_main = args.rtol if args.rtol else (1e-9 if prec_main == pkg.PRECISION_MIXED else 1e-12)
+    total_ms, outs, clocks = timed(prec_main, tol_main, args.steps, args.warmup)
     value = world * n_sig * args.steps / (total_ms / 1e3)
     st = outs[-1]["stats"]
     norm = outs[-1]["signal"] / outs[-1]["S0"]
+    kind = "mixed" if prec_main == pkg.PRECISION_MIXED else "fp64"
+    roof = roofline(kind, st)
+    launches = st["kernel_launches"]
 
-    # roofline of the dominant kernel (the persistent stepper)
-    iters_per_signal = st["total_iterations"] / n_sig
-    bytes_per_launch = alg_bytes_fp64(info["n_dofs"], info["nnz"], st["steps"], iters_per_signal)
-    launch_ms = st["stepper_ms"] / n_sig
-    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        peak = json.load(open(peaks_path))["hbm_gbs"]
-        peak_src = "measured"
-    else:
-        peak, peak_src = 6800.0, "fallback"
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        tr = json.load(open(tpath)).get(args.workload + ":" + args.precision)
-        if tr:
-            traffic = tr["bytes_per_launch"]
+    plain = None
+    if prec_main == pkg.PRECISION_MIXED and args.fp64_steps > 0:
+        t64, o64, c64 = timed(pkg.PRECISION_FP64, 1e-12, args.fp64_steps, max(1, min(args.warmup, 2)))
+        s64 = o64[-1]["stats"]
+        n64 = o64[-1]["signal"] / o64[-1]["S0"]
+        plain = {"value": world * n_sig * args.fp64_steps / (t64 / 1e3), "unit": "signals/s",
+                 "ms_per_step": t64 / args.fp64_steps, "steps": args.fp64_steps, "rtol": 1e-12,
+                 "normalized_signals": [float(v) for v in n64],
+                 "iterations_per_signal": s64["total_iterations"] / n_sig,
+                 "roofline": roofline("fp64", s64), "clocks": c64}
+        plain["mixed_over_plain"] = value / plain["value"]
+        plain["max_rel_err_mixed_vs_fp64"] = float(np.max(np.abs(norm - n64) / np.abs(n64)))
 
     # end to end through the public C-ABI from host buffers
     e2e_ms = []
     h2d = (w["xyz"].nbytes + w["tets"].astype(np.int32).nbytes + w["region"].astype(np.int32).nbytes
            + 8 * nr * (2 + nr) + fn.nbytes + fo.nbytes + q.nbytes + g.nbytes + pidx.nbytes)
     d2h = 8 * (n_sig + 1)
-    for _ in range(args.warmup_e2e):
-        pass
     for _ in range(args.e2e_steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -257,7 +312,7 @@ def gpu_run(args):
         c2.set_coefficients(w["D"], w["invT2"], w["kappa"])
         c2.assemble()
         c2.set_schedule(fn, fo, w["dt"])
-        o2 = c2.solve(q, g, pidx, None, prec, rtol, args.maxit)
+        o2 = c2.solve(q, g, pidx, None, prec_main, tol_main, args.maxit)
         _ = float(o2["signal"][0])                          # result on the host
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         c2.close()
@@ -267,33 +322,28 @@ def gpu_run(args):
     if rank == 0:
         cpu = cpu_baseline(args.workload, args.cpu_sample_steps, 1) if args.cpu_sample_steps > 0 else None
         res = {
-            "metric": "Bloch-Torrey signals/s on 1 GB300 (%s, %s)" % (args.workload, args.precision),
+            "metric": "Bloch-Torrey signals/s on 1 GB300 at <=1e-6 rel err (%s)" % args.workload,
             "value": value, "unit": "signals/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == pkg.PRECISION_FP64 else "f32+f64",
-            "data": "synthetic (seeded Kuhn box mesh and markers; no dataset)",
+            "vs_baseline": None,
+            "dtype": "f64" if kind == "fp64" else "f32 (inner COCG) + double-float residuals",
+            "data": "synthetic (seeded Kuhn box mesh and centroid markers; no dataset)",
             "config": {"workload": args.workload + ": " + WORKLOADS.get(args.workload, ""),
-                       "signals_per_step": n_sig, "precision": args.precision, "rtol": rtol,
+                       "signals_per_step": n_sig, "precision": kind, "rtol": tol_main,
                        "n_dofs": info["n_dofs"], "nnz": info["nnz"], "time_steps": st["steps"],
-                       "l2": "flushed between timed steps (512 MB write); the FP64 working set "
-                             "(%.0f MB) is L2-resident within a step" % (
-                                 (info["nnz"] * 24 + info["n_dofs"] * 16 * 8) / 1e6),
+                       "l2": "flushed between timed steps (512 MB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "normalized_signals": [float(v) for v in norm],
-            "iterations_per_signal": iters_per_signal,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_step64 (persistent FP64 CN/COCG stepper)",
-                         "bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
-                         "peak_source": peak_src + " hbm_gbs (copy)",
-                         "note": "working set L2-resident: achieved/HBM peak measures L2-served bytes"},
+            "iterations_per_signal": st["total_iterations"] / n_sig,
+            "roofline": roof,
+            "plain_fp64": plain,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "signals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
                     "what": "bt_create+bt_mesh_upload (device graph build)+bt_set_coefficients+bt_assemble+"
                             "bt_set_schedule+bt_solve, host arrays in, signals out; median of %d" % len(e2e_ms)},
-            "gpu_launches": int(st["kernel_launches"]) * args.steps,
-            "clocks": clk.summary(),
+            "gpu_launches": int(launches) * args.steps,
+            "clocks": clocks,
         }
         print(json.dumps(res))
     ctx.close()
@@ -313,7 +363,7 @@ def reference_run(args):
     for _ in range(args.ref_steps):
         vals.append(cpu_baseline(args.workload, args.cpu_sample_steps_ref, workers))
     v = statistics.median(x["value"] for x in vals)
-    out = {"metric": "Bloch-Torrey signals/s on 1 GB300 (%s, %s)" % (args.workload, args.precision),
+    out = {"metric": "Bloch-Torrey signals/s on 1 GB300 at <=1e-6 rel err (%s)" % args.workload,
            "value": v, "unit": "signals/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
            "steps": args.ref_steps, "warmup": 0, "higher_is_better": True, "scaling": "weak",
            "impl": "reference", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -331,7 +381,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 path (0: skip)")
     ap.add_argument("--rtol", type=float, default=None)
     ap.add_argument("--maxit", type=int, default=5000)
     ap.add_argument("--e2e-steps", type=int, default=3)

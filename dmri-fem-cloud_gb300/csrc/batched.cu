@@ -62,7 +62,7 @@ struct SolverMixed {
     DevBuf<double> w;         // per row signal weight
     DevBuf<int32_t> rcomp;
     DevBuf<float2> uh, ul, rh, rl, d0, d1, ri, z, p, q;  // [n][Rp]
-    DevBuf<double> partials, fin;
+    DevBuf<float2> partials, fin;   // double-float (hi, lo) sums
     DevBuf<double> sigpart;      // [warps][64][1+kMaxCompartments]
     DevBuf<unsigned> bar;
     DevBuf<int> status;
@@ -101,8 +101,8 @@ struct MixArgs {
     float4* z;
     float4* p;
     float4* q;
-    double* partials;
-    double* fin;
+    float2* partials;
+    float2* fin;
     double* sigpart;
     unsigned* bar;
     int* status;
@@ -190,23 +190,10 @@ __device__ __forceinline__ float2 cinvf(float2 b) { return cdivf(make_float2(1.0
 __device__ __forceinline__ bool cnonzero(float2 v) {
     return (v.x != 0.0f || v.y != 0.0f) && isfinite(v.x) && isfinite(v.y);
 }
-__device__ __forceinline__ bool cnonzero(double2 v) {
-    return (v.x != 0.0 || v.y != 0.0) && isfinite(v.x) && isfinite(v.y);
-}
-__device__ __forceinline__ float2 cdivf_d(double2 a, double2 b) {  // FP64 Smith division, FP32 result
-    if (fabs(b.x) >= fabs(b.y)) {
-        const double r = b.y / b.x, d = fma(b.y, r, b.x);
-        return make_float2((float)(fma(a.y, r, a.x) / d), (float)(fma(-a.x, r, a.y) / d));
-    }
-    const double r = b.x / b.y, d = fma(b.x, r, b.y);
-    return make_float2((float)(fma(a.x, r, a.y) / d), (float)(fma(a.y, r, -a.x) / d));
-}
-
 // Compensated (Kahan) FP32 accumulator.  The COCG scalars are sums of
-// products whose phases wind across the mesh (the gradient encodes position in
-// the phase), so they cancel by orders of magnitude; plain FP32 sequential sums
-// then lose the step length and COCG stalls.  Lanes accumulate compensated,
-// and every combination above the lane is done in FP64.
+// products that cancel strongly, and plain FP32 sequential sums then lose the
+// step length and COCG stalls.  Lanes accumulate compensated, and every
+// combination above the lane is done in double-float (reduce_rhs).
 struct KF {
     float s, c;
 };
@@ -218,25 +205,42 @@ __device__ __forceinline__ void kadd(KF& a, float x) {
 }
 
 // -------------------------------------------------------------- reductions ----
-// Each lane holds compensated sums v[2][kNV] for its two RHS.  On return out[][]
-// holds the grid-wide sums (FP64) for those RHS, bitwise identical in every block.
+// Each lane holds compensated sums v[2][kNV] for its two slots.  Lane sums are
+// combined as double-float pairs (error-free TwoSum), never in FP64, which is
+// slow on this GPU.  On return out[][] holds the grid-wide sums rounded to
+// FP32, bitwise identical in every block.
+__device__ __forceinline__ float2 dfa(float2 a, float2 b) {  // (hi, lo) + (hi, lo)
+    float s, e;
+    two_sum(a.x, b.x, s, e);
+    e += a.y + b.y;
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+
 template <int LPR>
-__device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], double (&out)[2][kNV], const MixArgs& a, int chunk,
-                                           int r0, unsigned nb, unsigned& gen, double* smem) {
+__device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV], const MixArgs& a, int chunk,
+                                           int r0, unsigned nb, unsigned& gen, float2* smem) {
     constexpr int C = 2 * LPR;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    double d[2][kNV];
+    float2 d[2][kNV];
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
-        for (int k = 0; k < kNV; ++k) d[j][k] = (double)v[j][k].s - (double)v[j][k].c;
+        for (int k = 0; k < kNV; ++k) {
+            const float h = v[j][k].s - v[j][k].c;   // Kahan: true sum = s - c
+            d[j][k] = make_float2(h, (v[j][k].s - h) - v[j][k].c);
+        }
     // combine the row slots of the warp
 #pragma unroll
     for (int o = 16; o >= LPR; o >>= 1) {
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) d[j][k] += __shfl_xor_sync(0xffffffffu, d[j][k], o);
+            for (int k = 0; k < kNV; ++k) {
+                const float2 t = make_float2(__shfl_xor_sync(0xffffffffu, d[j][k].x, o),
+                                             __shfl_xor_sync(0xffffffffu, d[j][k].y, o));
+                d[j][k] = dfa(d[j][k], t);
+            }
     }
     if (lane < LPR) {
 #pragma unroll
@@ -246,13 +250,13 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], double (&out)[2][kNV
     }
     __syncthreads();
     const int nchunks = a.Rp / C;
-    // block partial for every RHS: sum over this block's warps of that chunk, in order
+    // block partial for every slot: sum over this block's warps of that chunk, in order
     for (int t = threadIdx.x; t < a.Rp * kNV; t += blockDim.x) {
         const int r = t / kNV, k = t % kNV;
         const int c = r / C, o = r % C;
-        double s = 0.0;
+        float2 s = make_float2(0.f, 0.f);
         for (int wb = 0; wb < kWarpsB; ++wb)
-            if ((int)((blockIdx.x * kWarpsB + wb) % nchunks) == c) s += smem[(wb * C + o) * kNV + k];
+            if ((int)((blockIdx.x * kWarpsB + wb) % nchunks) == c) s = dfa(s, smem[(wb * C + o) * kNV + k]);
         a.partials[(size_t)blockIdx.x * a.Rp * kNV + t] = s;
     }
     if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
@@ -260,28 +264,31 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], double (&out)[2][kNV
         // stage 2: grid threads each finish some (r, k) in block order
         const int gt = blockIdx.x * blockDim.x + threadIdx.x;
         for (int t = gt; t < a.Rp * kNV; t += nb * blockDim.x) {
-            double s = 0.0;
-            for (unsigned b = 0; b < nb; ++b) s += __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]);
+            float2 s = make_float2(0.f, 0.f);
+            for (unsigned b = 0; b < nb; ++b) s = dfa(s, __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]));
             a.fin[t] = s;
         }
         if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) out[j][k] = __ldcg(&a.fin[(r0 + j) * kNV + k]);
+            for (int k = 0; k < kNV; ++k) {
+                const float2 f = __ldcg(&a.fin[(r0 + j) * kNV + k]);
+                out[j][k] = f.x + f.y;
+            }
     } else {
         // one stage: each block sums all partials (few) into shared memory
         __syncthreads();
         for (int t = threadIdx.x; t < a.Rp * kNV; t += blockDim.x) {
-            double s = 0.0;
-            for (unsigned b = 0; b < nb; ++b) s += __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]);
+            float2 s = make_float2(0.f, 0.f);
+            for (unsigned b = 0; b < nb; ++b) s = dfa(s, __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]));
             smem[t] = s;
         }
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) out[j][k] = smem[(r0 + j) * kNV + k];
+            for (int k = 0; k < kNV; ++k) out[j][k] = smem[(r0 + j) * kNV + k].x + smem[(r0 + j) * kNV + k].y;
     }
     __syncthreads();
     return true;
@@ -292,7 +299,7 @@ template <int LPR>
 __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
     constexpr int G = 32 / LPR;  // rows per warp-unit
     constexpr int C = 2 * LPR;   // RHS per warp-unit
-    __shared__ double smem[kWarpsB * 64 * kNV > kMaxRhs * kNV ? kWarpsB * 64 * kNV : kMaxRhs * kNV];
+    __shared__ float2 smem[kWarpsB * 64 * kNV > kMaxRhs * kNV ? kWarpsB * 64 * kNV : kMaxRhs * kNV];
     __shared__ int s_flag;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kWarpsB + (threadIdx.x >> 5);
@@ -320,8 +327,8 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
         sq[j] = a.seqv[r0 + j];
     }
     // partial buffers alternate between consecutive reductions (see reduce_rhs)
-    double* const part0 = a.partials;
-    double* const part1 = a.partials + (size_t)nb * a.Rp * kNV;
+    float2* const part0 = a.partials;
+    float2* const part1 = a.partials + (size_t)nb * a.Rp * kNV;
     unsigned flip = 0;
     MixArgs b = a;
 #define BT_REDUCE(V, OUT)                                                     \
@@ -401,16 +408,16 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
             kadd(red[0][3], bn);
             kadd(red[1][3], bn);
         }
-        double rs[2][kNV];
+        float rs[2][kNV];
         BT_REDUCE(red, rs);
-        double2 rho[2];
-        double rr2[2], tolb2[2], rrs[2];
+        float2 rho[2];
+        float rr2[2], tolb2[2], rrs[2];
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            rho[j] = make_double2(rs[j][0], rs[j][1]);
+            rho[j] = make_float2(rs[j][0], rs[j][1]);
             rr2[j] = rs[j][2];
             rrs[j] = rs[j][2];
-            tolb2[j] = (double)a.rtol * (double)a.rtol * rs[j][3];   // (rtol ||b||)^2
+            tolb2[j] = a.rtol * a.rtol * rs[j][3];   // (rtol ||b||)^2
         }
         int sweep = 0, it_total = 0;
         bool failed = false;
@@ -424,7 +431,7 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                 // lane-local activity of its two RHS; grid decision via s_flag below
 #pragma unroll
                 for (int j = 0; j < 2; ++j)
-                    act[j] = (r0 + j < a.R) && rr2[j] > (double)eps * eps * rrs[j] && rr2[j] > 0.09 * tolb2[j];
+                    act[j] = (r0 + j < a.R) && rr2[j] > eps * eps * rrs[j] && rr2[j] > 0.09f * tolb2[j];
                 if (threadIdx.x == 0) s_flag = 0;
                 __syncthreads();
                 if (act[0] || act[1]) s_flag = 1;
@@ -437,7 +444,7 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                     for (int j = 0; j < 2; ++j)
                         if (blockIdx.x == 0 && act[j]) {
                             a.diag[0] = 1.0f; a.diag[1] = (float)step; a.diag[2] = (float)sweep; a.diag[3] = (float)it;
-                            a.diag[4] = (float)(rr2[j] / fmax((double)eps * eps * rrs[j], 1e-300));
+                            a.diag[4] = rr2[j] / fmaxf(eps * eps * rrs[j], 1e-38f);
                             a.diag[5] = (float)(r0 / 2);
                         }
                     failed = true;
@@ -456,10 +463,7 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
 #pragma unroll
                     for (int j = 0; j < 2; ++j) sA[j] = sx[j] = sy[j] = sz[j] = make_float2(0.f, 0.f);
                     const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
-                    for (int e = e0; e < e1; ++e) {
-                        const int cidx = a.col[e];
-                        const float4 m = a.mA[e];
-                        const float4 zz = a.z[(size_t)cidx * Rp4 + c4];
+                    auto acc_entry = [&](const float4 m, const float4 zz) {
                         const float2 zj[2] = {make_float2(zz.x, zz.y), make_float2(zz.z, zz.w)};
 #pragma unroll
                         for (int j = 0; j < 2; ++j) {
@@ -468,7 +472,23 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                             sy[j].x = fmaf(m.z, zj[j].x, sy[j].x); sy[j].y = fmaf(m.z, zj[j].y, sy[j].y);
                             sz[j].x = fmaf(m.w, zj[j].x, sz[j].x); sz[j].y = fmaf(m.w, zj[j].y, sz[j].y);
                         }
+                    };
+                    int e = e0;
+                    // four independent neighbour gathers in flight per warp
+                    for (; e + 4 <= e1; e += 4) {
+                        int cc[4];
+                        float4 mm[4], zz[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            cc[u] = a.col[e + u];
+                            mm[u] = a.mA[e + u];
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) zz[u] = a.z[(size_t)cc[u] * Rp4 + c4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) acc_entry(mm[u], zz[u]);
                     }
+                    for (; e < e1; ++e) acc_entry(a.mA[e], a.z[(size_t)a.col[e] * Rp4 + c4]);
                     const size_t vi = (size_t)row * Rp4 + c4;
                     const float4 zo = a.z[vi], po = a.p[vi], qo = a.q[vi];
                     const float zov[4] = {zo.x, zo.y, zo.z, zo.w}, pov[4] = {po.x, po.y, po.z, po.w},
@@ -492,15 +512,15 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                     a.p[vi] = make_float4(pn[0], pn[1], pn[2], pn[3]);
                     a.q[vi] = make_float4(qn[0], qn[1], qn[2], qn[3]);
                 }
-                double ms[2][kNV];
+                float ms[2][kNV];
                 BT_REDUCE(mu, ms);
                 float2 alpha[2];
 #pragma unroll
                 for (int j = 0; j < 2; ++j) {
-                    const double2 m2 = make_double2(ms[j][0], ms[j][1]);
-                    // inactive or broken-down RHS take no step (its residual stays put;
+                    const float2 m2 = make_float2(ms[j][0], ms[j][1]);
+                    // inactive or broken-down slots take no step (the residual stays put;
                     // the outer check reports it if it never converges)
-                    alpha[j] = (act[j] && cnonzero(m2) && cnonzero(rho[j])) ? cdivf_d(rho[j], m2)
+                    alpha[j] = (act[j] && cnonzero(m2) && cnonzero(rho[j])) ? cdivf(rho[j], m2)
                                                                            : make_float2(0.f, 0.f);
                 }
                 // phase B: d += alpha p ; r -= alpha q ; z = D^-1 r
@@ -539,12 +559,12 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                     a.ri[vi] = make_float4(rn[0], rn[1], rn[2], rn[3]);
                     a.z[vi] = make_float4(zn[0], zn[1], zn[2], zn[3]);
                 }
-                double rbs[2][kNV];
+                float rbs[2][kNV];
                 BT_REDUCE(rb, rbs);
 #pragma unroll
                 for (int j = 0; j < 2; ++j) {
-                    const double2 rn2 = make_double2(rbs[j][0], rbs[j][1]);
-                    beta[j] = (act[j] && cnonzero(rho[j])) ? cdivf_d(rn2, rho[j]) : make_float2(0.f, 0.f);
+                    const float2 rn2 = make_float2(rbs[j][0], rbs[j][1]);
+                    beta[j] = (act[j] && cnonzero(rho[j])) ? cdivf(rn2, rho[j]) : make_float2(0.f, 0.f);
                     if (act[j]) {
                         rho[j] = rn2;
                         rr2[j] = rbs[j][2];
@@ -617,14 +637,14 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                 kadd(ru[1][1], ni.h * z1.y);
                 kadd(ru[1][2], ni.h * ni.h);
             }
-            double rus[2][kNV];
+            float rus[2][kNV];
             BT_REDUCE(ru, rus);
             dsel ^= 1;
             ++sweep;
             bool more = false;
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
-                rho[j] = make_double2(rus[j][0], rus[j][1]);
+                rho[j] = make_float2(rus[j][0], rus[j][1]);
                 rr2[j] = rus[j][2];
                 rrs[j] = rus[j][2];
             }
@@ -639,7 +659,7 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                 if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
                 if (blockIdx.x == 0 && r0 < a.R && rr2[0] + rr2[1] > tolb2[0]) {
                     a.diag[0] = 2.0f; a.diag[1] = (float)step; a.diag[2] = (float)sweep; a.diag[3] = (float)it_total;
-                    a.diag[4] = (float)((rr2[0] + rr2[1]) / fmax(tolb2[0], 1e-300)); a.diag[5] = (float)(r0 / 2);
+                    a.diag[4] = (rr2[0] + rr2[1]) / fmaxf(tolb2[0], 1e-38f); a.diag[5] = (float)(r0 / 2);
                 }
                 failed = true;
                 break;

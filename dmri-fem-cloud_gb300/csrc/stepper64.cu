@@ -210,11 +210,29 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
             for (int s = gw; s < a.n_slices; s += total_warps) {
                 const int32_t base = a.sl_ptr[s], wdt = a.sl_w[s];
                 double2 sA = make_double2(0.0, 0.0), sJ = sA;
-                for (int k = 0; k < wdt; ++k) {
+                int k = 0;
+                // four independent neighbour gathers in flight per thread
+                for (; k + 4 <= wdt; k += 4) {
+                    int32_t cc[4];
+                    double2 mm[4], zz[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int32_t e = base + (k + u) * 32 + lane;
+                        cc[u] = a.col[e];
+                        mm[u] = a.aj[e];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) zz[u] = a.z[cc[u]];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        sA.x = fma(mm[u].x, zz[u].x, sA.x); sA.y = fma(mm[u].x, zz[u].y, sA.y);
+                        sJ.x = fma(mm[u].y, zz[u].x, sJ.x); sJ.y = fma(mm[u].y, zz[u].y, sJ.y);
+                    }
+                }
+                for (; k < wdt; ++k) {
                     const int32_t e = base + k * 32 + lane;
-                    const int32_t c = a.col[e];
                     const double2 m = a.aj[e];
-                    const double2 zc = a.z[c];
+                    const double2 zc = a.z[a.col[e]];
                     sA.x = fma(m.x, zc.x, sA.x); sA.y = fma(m.x, zc.y, sA.y);
                     sJ.x = fma(m.y, zc.x, sJ.x); sJ.y = fma(m.y, zc.y, sJ.y);
                 }
