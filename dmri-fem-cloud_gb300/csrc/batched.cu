@@ -260,13 +260,18 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
         a.partials[(size_t)blockIdx.x * a.Rp * kNV + t] = s;
     }
     if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
+    const int V = a.Rp * kNV;
     if (a.two_stage) {
-        // stage 2: grid threads each finish some (r, k) in block order
-        const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-        for (int t = gt; t < a.Rp * kNV; t += nb * blockDim.x) {
+        // stage 2: one warp per value; lane l adds blocks l, l+32, ... and the
+        // warp combines the 32 lane sums in a fixed butterfly (lane 0's order)
+        const int gw = blockIdx.x * kWarpsB + wib;
+        for (int t = gw; t < V; t += nb * kWarpsB) {
             float2 s = make_float2(0.f, 0.f);
-            for (unsigned b = 0; b < nb; ++b) s = dfa(s, __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]));
-            a.fin[t] = s;
+            for (unsigned b = lane; b < nb; b += 32) s = dfa(s, __ldcg(&a.partials[(size_t)b * V + t]));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                s = dfa(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
+            if (lane == 0) a.fin[t] = s;
         }
         if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
 #pragma unroll
@@ -277,12 +282,21 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
                 out[j][k] = f.x + f.y;
             }
     } else {
-        // one stage: each block sums all partials (few) into shared memory
+        // one stage: each block sums all partials (few values) into shared
+        // memory; G lanes per value stride over the blocks and combine in a
+        // fixed butterfly, so every block forms bitwise the same sums
         __syncthreads();
-        for (int t = threadIdx.x; t < a.Rp * kNV; t += blockDim.x) {
+        int G = 32;
+        while (G > 1 && V * G > (int)blockDim.x) G >>= 1;
+        const int part = threadIdx.x % G;
+        for (int t0 = 0; t0 < V; t0 += blockDim.x / G) {
+            const int t = t0 + threadIdx.x / G;
             float2 s = make_float2(0.f, 0.f);
-            for (unsigned b = 0; b < nb; ++b) s = dfa(s, __ldcg(&a.partials[(size_t)b * a.Rp * kNV + t]));
-            smem[t] = s;
+            if (t < V)
+                for (unsigned b = part; b < nb; b += G) s = dfa(s, __ldcg(&a.partials[(size_t)b * V + t]));
+            for (int o = G / 2; o > 0; o >>= 1)
+                s = dfa(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
+            if (part == 0 && t < V) smem[t] = s;
         }
         __syncthreads();
 #pragma unroll
