@@ -32,7 +32,7 @@ EXPORTS = [
     "bt_mesh_upload", "bt_mesh_info", "bt_set_coefficients", "bt_set_cell_diffusion",
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
-    "bt_signal_noalloc",
+    "bt_signal_noalloc", "bt_adjoint",
 ]
 
 
@@ -101,6 +101,8 @@ def load(path=None):
         "bt_get_iterations": (C.c_int, [_P, _I32, C.c_int64]),
         "bt_set_option": (C.c_int, [_P, C.c_char_p, C.c_double]),
         "bt_signal_noalloc": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
+        "bt_adjoint": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_double, C.c_int32, C.c_int32,
+                                 _D, _D, _D, _D, C.POINTER(Stats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -218,6 +220,22 @@ class Context:
         if compartments:
             out["compartments"] = comp.reshape(n, self.n_compartments)
         return out
+
+    def adjoint(self, q, gdir, sequence=0, u0=None, rtol=1e-13, max_iterations=5000, stride=0):
+        """Signal and its derivatives (unnormalised) w.r.t. per-region D, 1/T2
+        and pair permeabilities, by the discrete adjoint of the FP64 solve."""
+        g = np.ascontiguousarray(np.asarray(gdir, np.float64).reshape(3))
+        u = None if u0 is None else np.ascontiguousarray(np.asarray(u0, np.float64).reshape(self.n_vertices))
+        nr = self.n_regions
+        sig = np.zeros(1)
+        dD, dT = np.zeros(nr), np.zeros(nr)
+        dK = np.zeros(nr * nr)
+        st = Stats()
+        self._check(self.lib.bt_adjoint(self.h, float(q), _dp(g), int(sequence), _dp(u), float(rtol),
+                                        int(max_iterations), int(stride), _dp(sig), _dp(dD), _dp(dT), _dp(dK),
+                                        C.byref(st)))
+        return {"signal": float(sig[0]), "dD": dD, "dinvT2": dT, "dkappa": dK.reshape(nr, nr),
+                "stats": st.as_dict()}
 
     def csr(self):
         inf = self.info()

@@ -263,6 +263,28 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
     });
 }
 
+int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0, double rtol,
+               int32_t max_iterations, int32_t checkpoint_stride, double* signal_out, double* dS_dD,
+               double* dS_dinvT2, double* dS_dkappa, bt_stats* stats) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint: mesh not assembled");
+        BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_adjoint: no schedule");
+        BT_REQUIRE(gdir && signal_out, BT_ERR_INVALID, "bt_adjoint: bad arguments");
+        BT_REQUIRE(std::isfinite(q) && std::isfinite(gdir[0]) && std::isfinite(gdir[1]) && std::isfinite(gdir[2]),
+                   BT_ERR_INVALID, "bt_adjoint: q and gdir must be finite");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_adjoint: rtol must be > 0 and max_iterations >= 1");
+        if (u0)
+            for (int64_t v = 0; v < ctx->mesh.n_v; ++v)
+                BT_REQUIRE(std::isfinite(u0[v]), BT_ERR_INVALID, "bt_adjoint: u0 must be finite");
+        use_device(ctx);
+        bt::adjoint_fp64(ctx, q, gdir, sequence, u0, rtol, max_iterations, checkpoint_stride, signal_out, dS_dD,
+                         dS_dinvT2, dS_dkappa, stats);
+        ctx->last_precision = -1;
+    });
+}
+
 int bt_set_option(bt_ctx* ctx, const char* key, double value) {
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {

@@ -114,6 +114,7 @@ struct Mesh {
     DevBuf<int32_t> nbr;              // [n_t*4] cell across face a (opposite local vertex a), -1 boundary
     DevBuf<int32_t> row_ptr, col;     // CSR
     DevBuf<int32_t> diag_pos;         // CSR position of the diagonal of each row
+    DevBuf<int32_t> iface_cell, iface_face;  // interface facets: owning (lower-index) cell, local face
     // cell colouring
     int32_t n_colours = 0;
     std::vector<int32_t> colour_ptr;  // host, n_colours+1
@@ -187,6 +188,9 @@ void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir,
                  const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig,
                  bt_stats* st);
 void get_solution_fp64(bt_ctx* ctx, int32_t index, double* u);
+void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const double* u0, double rtol,
+                  int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
+                  bt_stats* st);
 void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u);
 void free_solvers(bt_ctx* ctx);
 double device_sum(const double* d, int64_t n, cudaStream_t s);

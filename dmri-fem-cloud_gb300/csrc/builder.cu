@@ -504,13 +504,18 @@ void build_graph(bt_ctx* ctx, const double* xyz, int64_t n_v, const int32_t* tet
         std::vector<int32_t> hn(n_t * 4);
         m.nbr.download(hn.data(), n_t * 4, s);
         BT_CUDA(cudaStreamSynchronize(s));
-        int64_t ni = 0;
+        std::vector<int32_t> fc, ff;
         for (int64_t i = 0; i < n_t * 4; ++i) {
             int32_t nb = hn[i];
             int64_t t = i >> 2;
-            if (nb > t && comp[nb] != comp[t]) ++ni;
+            if (nb > t && comp[nb] != comp[t]) {
+                fc.push_back((int32_t)t);
+                ff.push_back((int32_t)(i & 3));
+            }
         }
-        m.n_iface = ni;
+        m.n_iface = (int64_t)fc.size();
+        m.iface_cell.upload(fc.data(), fc.size(), s);
+        m.iface_face.upload(ff.data(), ff.size(), s);
     }
 
     // 5. Jones-Plassmann colouring

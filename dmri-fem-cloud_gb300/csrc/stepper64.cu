@@ -89,6 +89,10 @@ struct StepArgs {
     int32_t nc;
     int32_t extrapolate;
     double rtol2;
+    const double* __restrict__ rhs_vec;  // nullable: right-hand side b = rhs_vec (real) for step 0
+    double2* save;                       // nullable: state after step s saved to save[(s+1)/save_every - 1]
+    int32_t save_every;
+    int64_t n_pad;
     int32_t* iters;
     double* relres;
     double* out;
@@ -169,9 +173,10 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 tJ.x = fma(m.y, vj.x, tJ.x); tJ.y = fma(m.y, vj.y, tJ.y);
             }
             const int64_t i = (int64_t)s * 32 + lane;
-            const double2 b = make_double2(fma(co, sJ.y, sB.x), fma(-co, sJ.x, sB.y));
+            const double2 b = (a.rhs_vec && step == 0) ? make_double2(a.rhs_vec[i], 0.0)
+                                                       : make_double2(fma(co, sJ.y, sB.x), fma(-co, sJ.x, sB.y));
             // A x0 with x0 = 2 u_n - u_{n-1} (or u_n)
-            const double ex = a.extrapolate ? 1.0 : 0.0;
+            const double ex = (a.extrapolate && !(a.rhs_vec && step == 0)) ? 1.0 : 0.0;
             const double2 gA = make_double2(sA.x + ex * (sA.x - tA.x), sA.y + ex * (sA.y - tA.y));
             const double2 gJ = make_double2(sJ.x + ex * (sJ.x - tJ.x), sJ.y + ex * (sJ.y - tJ.y));
             const double2 ax = make_double2(fma(-cn, gJ.y, gA.x), fma(cn, gJ.x, gA.y));
@@ -296,6 +301,13 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
         if (failed) return;
         // The last phase B (or phase R when no iteration ran) ended in a grid
         // barrier, so u_{n+1} is complete before the next phase R gathers it.
+        if (a.save && ((step + 1) % a.save_every) == 0) {
+            double2* dst = a.save + (int64_t)((step + 1) / a.save_every - 1) * a.n_pad;
+            for (int s = gw; s < a.n_slices; s += total_warps) {
+                const int64_t i = (int64_t)s * 32 + lane;
+                dst[i] = x[i];
+            }
+        }
     }
     // ---- signal: S = sum w Re(u_N), per compartment
     double acc[kRed];
@@ -377,15 +389,10 @@ static void map_status(int st) {
     }
 }
 
-void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
-                const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st) {
+// Allocate the FP64 workspace for a mesh and a schedule of n_steps.
+static void prepare_fp64(bt_ctx* ctx, Solver64& W) {
     Mesh& m = ctx->mesh;
-    Assembled& A = ctx->mat;
     Schedule& S = ctx->sched;
-    cudaStream_t s = ctx->stream;
-    if (!ctx->s64) ctx->s64 = new Solver64();
-    Solver64& W = *ctx->s64;
-    const int64_t n = m.n_dofs;
     W.n_pad = (int64_t)m.n_slices * 32;
     W.sell = m.sell_entries;
     W.aj.alloc(W.sell);
@@ -400,22 +407,117 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
     W.iters.alloc(S.n_steps);
     W.out.alloc(kRed);
     W.gq.alloc(3);
-    W.saved.alloc((size_t)nsig * W.n_pad);
-    W.saved_nsig = nsig;
-    DevBuf<double> d_u0;
-    if (u0) d_u0.upload(u0, m.n_v, s);
-
-    // grid: co-resident blocks, no more than the slices need
     int per_sm = 0;
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step64, kThreads64, 0));
     BT_REQUIRE(per_sm >= 1, BT_ERR_CUDA, "stepper kernel does not fit on an SM");
     const int need = (m.n_slices + kThreads64 / 32 - 1) / (kThreads64 / 32);
     W.nblocks = std::max(1, std::min(per_sm * ctx->num_sms, need));
     W.partials.alloc((size_t)2 * W.nblocks * kRed);
+}
 
+// Pack the matrix of one signal (direction g, theta, dt), the row data, and the
+// initial state u0 into u[0] and u[2] (so the first step does not extrapolate).
+static void pack_signal_fp64(bt_ctx* ctx, Solver64& W, const double* gdir, const double* d_u0) {
+    Mesh& m = ctx->mesh;
+    Assembled& A = ctx->mat;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
     const double inv_k = 1.0 / S.dt;
-    std::vector<double> hcn(S.n_steps), hco(S.n_steps), hout(kRed), hres(S.n_steps);
-    std::vector<int32_t> hit(S.n_steps);
+    W.gq.upload(gdir, 3, s);
+    k_pack64<<<(unsigned)((W.sell + 255) / 256), 256, 0, s>>>(W.sell, m.sl_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy,
+                                                             A.Jz, W.gq, inv_k, S.theta, W.aj, W.bre);
+    k_rows64<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(
+        m.n_dofs, W.n_pad, m.diag_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz, W.gq, inv_k, S.theta, A.w, m.dof_comp,
+        m.dof_vertex, d_u0, W.dA, W.dJ, W.w, W.rcomp, W.u[0], W.u[2], W.u[1]);
+    BT_CUDA(cudaGetLastError());
+}
+
+// One cooperative launch of k_step64 over n_steps steps with the schedule
+// d_cn[0..n_steps), d_co[...]; the state enters in u[0] (u[2] = previous
+// level) and leaves in u[n_steps % 3].  Returns the launch's device time.
+static float run_steps_fp64(bt_ctx* ctx, Solver64& W, const double* d_cn, const double* d_co, int n_steps,
+                            bool extrapolate, const double* rhs_vec, double2* save, int save_every, double rtol,
+                            int maxit, std::vector<int32_t>* iters_out, std::vector<double>* relres_out,
+                            double* out_sig) {
+    Mesh& m = ctx->mesh;
+    cudaStream_t s = ctx->stream;
+    W.bar.zero(s);
+    W.status.zero(s);
+    StepArgs a;
+    a.n_slices = m.n_slices;
+    a.sl_ptr = m.sl_ptr; a.sl_w = m.sl_w; a.col = m.sl_col;
+    a.aj = W.aj; a.bre = W.bre; a.dA = W.dA; a.dJ = W.dJ; a.w = W.w; a.rcomp = W.rcomp;
+    a.u0 = W.u[0]; a.u1 = W.u[1]; a.u2 = W.u[2];
+    a.r = W.r; a.z = W.z; a.p = W.p; a.q = W.q; a.dinv = W.dinv;
+    a.partials = W.partials; a.bar = W.bar; a.status = W.status;
+    a.cn = d_cn; a.co = d_co;
+    a.n_steps = n_steps;
+    a.maxit = maxit;
+    a.nc = m.n_comp;
+    a.extrapolate = extrapolate ? 1 : 0;
+    a.rtol2 = rtol * rtol;
+    a.rhs_vec = rhs_vec;
+    a.save = save;
+    a.save_every = save_every > 0 ? save_every : 1;
+    a.n_pad = W.n_pad;
+    a.iters = W.iters; a.relres = W.relres; a.out = W.out;
+    {
+        const void* need_ptrs[] = {a.sl_ptr, a.sl_w, a.col, a.aj, a.bre, a.dA, a.dJ, a.w, a.rcomp, a.u0, a.u1,
+                                   a.u2, a.r, a.z, a.p, a.q, a.dinv, a.partials, a.bar, a.status, a.cn, a.co,
+                                   a.iters, a.relres, a.out};
+        for (const void* ptr : need_ptrs)
+            BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "stepper: a device buffer is not allocated");
+        BT_REQUIRE(n_steps >= 1 && (size_t)n_steps <= W.iters.n, BT_ERR_INVALID, "stepper: bad step count");
+    }
+    void* args[] = {&a};
+    BT_CUDA(cudaEventRecord(ctx->ev1, s));
+    BT_CUDA(cudaLaunchCooperativeKernel((const void*)k_step64, dim3(W.nblocks), dim3(kThreads64), args, 0, s));
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    int hst = 0;
+    BT_CUDA(cudaMemcpyAsync(&hst, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (iters_out) {
+        iters_out->resize(n_steps);
+        W.iters.download(iters_out->data(), n_steps, s);
+    }
+    if (relres_out) {
+        relres_out->resize(n_steps);
+        W.relres.download(relres_out->data(), n_steps, s);
+    }
+    if (out_sig) W.out.download(out_sig, kRed, s);
+    BT_CUDA(cudaStreamSynchronize(s));
+    map_status(hst);
+    float ms = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
+    return ms;
+}
+
+static void schedule_row(const Schedule& S, int32_t row, double q, std::vector<double>& hcn,
+                         std::vector<double>& hco) {
+    BT_REQUIRE(row >= 0 && row < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
+    const double* fn = S.f_new.data() + (size_t)row * S.n_steps;
+    const double* fo = S.f_old.data() + (size_t)row * S.n_steps;
+    hcn.resize(S.n_steps);
+    hco.resize(S.n_steps);
+    for (int k = 0; k < S.n_steps; ++k) {
+        hcn[k] = S.theta * q * fn[k];
+        hco[k] = (1.0 - S.theta) * q * fo[k];
+    }
+}
+
+void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
+                const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st) {
+    Mesh& m = ctx->mesh;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    if (!ctx->s64) ctx->s64 = new Solver64();
+    Solver64& W = *ctx->s64;
+    prepare_fp64(ctx, W);
+    W.saved.alloc((size_t)nsig * W.n_pad);
+    W.saved_nsig = nsig;
+    DevBuf<double> d_u0;
+    if (u0) d_u0.upload(u0, m.n_v, s);
+    std::vector<double> hcn, hco, hout(kRed), hres;
+    std::vector<int32_t> hit;
     ctx->last_iters.assign((size_t)nsig * S.n_steps, 0);
     if (st) {
         st->steps = S.n_steps;
@@ -430,62 +532,14 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
     float stepper_ms_total = 0.0f;
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
     for (int32_t sg = 0; sg < nsig; ++sg) {
-        const int32_t row = seq ? seq[sg] : 0;
-        BT_REQUIRE(row >= 0 && row < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
-        const double* fn = S.f_new.data() + (size_t)row * S.n_steps;
-        const double* fo = S.f_old.data() + (size_t)row * S.n_steps;
-        for (int k = 0; k < S.n_steps; ++k) {
-            hcn[k] = S.theta * q[sg] * fn[k];
-            hco[k] = (1.0 - S.theta) * q[sg] * fo[k];
-        }
+        schedule_row(S, seq ? seq[sg] : 0, q[sg], hcn, hco);
         W.cn.upload(hcn.data(), S.n_steps, s);
         W.co.upload(hco.data(), S.n_steps, s);
-        W.gq.upload(gdir + 3 * sg, 3, s);
-        k_pack64<<<(unsigned)((W.sell + 255) / 256), 256, 0, s>>>(W.sell, m.sl_pos, A.M, A.K, A.T, A.R, A.Jx,
-                                                                 A.Jy, A.Jz, W.gq, inv_k, S.theta, W.aj, W.bre);
-        k_rows64<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(
-            n, W.n_pad, m.diag_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz, W.gq, inv_k, S.theta, A.w, m.dof_comp,
-            m.dof_vertex, u0 ? d_u0.p : nullptr, W.dA, W.dJ, W.w, W.rcomp, W.u[0], W.u[2], W.u[1]);
-        BT_CUDA(cudaGetLastError());
-        W.bar.zero(s);
-        W.status.zero(s);
-        StepArgs a;
-        a.n_slices = m.n_slices;
-        a.sl_ptr = m.sl_ptr; a.sl_w = m.sl_w; a.col = m.sl_col;
-        a.aj = W.aj; a.bre = W.bre; a.dA = W.dA; a.dJ = W.dJ; a.w = W.w; a.rcomp = W.rcomp;
-        a.u0 = W.u[0]; a.u1 = W.u[1]; a.u2 = W.u[2];
-        a.r = W.r; a.z = W.z; a.p = W.p; a.q = W.q; a.dinv = W.dinv;
-        a.partials = W.partials; a.bar = W.bar; a.status = W.status;
-        a.cn = W.cn; a.co = W.co;
-        a.n_steps = S.n_steps;
-        a.maxit = maxit;
-        a.nc = m.n_comp;
-        a.extrapolate = ctx->opt_fp64_extrapolate;
-        a.rtol2 = rtol * rtol;
-        a.iters = W.iters; a.relres = W.relres; a.out = W.out;
-        {
-            const void* need_ptrs[] = {a.sl_ptr, a.sl_w, a.col, a.aj, a.bre, a.dA, a.dJ, a.w, a.rcomp, a.u0, a.u1,
-                                       a.u2, a.r, a.z, a.p, a.q, a.dinv, a.partials, a.bar, a.status, a.cn, a.co,
-                                       a.iters, a.relres, a.out};
-            for (const void* ptr : need_ptrs)
-                BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "stepper: a device buffer is not allocated");
-        }
-        void* args[] = {&a};
-        BT_CUDA(cudaEventRecord(ctx->ev1, s));
-        BT_CUDA(cudaLaunchCooperativeKernel((const void*)k_step64, dim3(W.nblocks), dim3(kThreads64), args, 0, s));
-        BT_CUDA(cudaEventRecord(ctx->ev2, s));
+        pack_signal_fp64(ctx, W, gdir + 3 * sg, u0 ? d_u0.p : nullptr);
+        stepper_ms_total += run_steps_fp64(ctx, W, W.cn, W.co, S.n_steps, ctx->opt_fp64_extrapolate != 0, nullptr,
+                                           nullptr, 1, rtol, maxit, &hit, &hres, hout.data());
         BT_CUDA(cudaMemcpyAsync(W.saved.p + (size_t)sg * W.n_pad, W.u[S.n_steps % 3].p,
                                 W.n_pad * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        int hst = 0;
-        BT_CUDA(cudaMemcpyAsync(&hst, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-        W.out.download(hout.data(), kRed, s);
-        W.iters.download(hit.data(), S.n_steps, s);
-        W.relres.download(hres.data(), S.n_steps, s);
-        BT_CUDA(cudaStreamSynchronize(s));
-        float ms = 0.0f;
-        BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
-        stepper_ms_total += ms;
-        map_status(hst);
         sig[sg] = hout[0];
         if (comp_sig)
             for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)sg * m.n_comp + c] = hout[1 + c];
@@ -522,6 +576,289 @@ void get_solution_fp64(bt_ctx* ctx, int32_t index, double* u) {
 void free_solver64(bt_ctx* ctx) {
     delete ctx->s64;
     ctx->s64 = nullptr;
+}
+
+}  // namespace bt
+
+namespace bt {
+
+// ============================================================== adjoint ====
+// Discrete adjoint of the FP64 Crank-Nicolson loop (spec form (3)).
+//
+//   forward   A_n u_{n+1} = B_n u_n,   Sig = Re(w^T u_N)
+//   adjoint   lambda_N = A_{N-1}^{-1} w,  lambda_n = A_{n-1}^{-1} B_n lambda_{n+1}
+//   gradient  dSig/dxi = -Re sum_n lambda_{n+1}^T (dS/dxi) (theta u_{n+1} + (1-theta) u_n)
+//
+// A and B are complex symmetric, so the transposed solves are the same COCG
+// steps run on a shifted schedule.  S = K + T + R is linear in every
+// parameter: D_r (isotropic, per region), 1/T2_r and kappa of each region pair,
+// so dS/dxi is the unit-coefficient element (or facet) matrix of the cells
+// (facets) carrying xi; the contraction is done per cell / per interface facet
+// and accumulated over steps on the device, then reduced once in index order.
+// Forward states are recomputed from checkpoints every `stride` steps
+// (default ceil(sqrt(N))).
+namespace {
+
+__global__ void k_adj_cells(int64_t n_t, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                            const int32_t* __restrict__ comp, const int32_t* __restrict__ dof_of, int nc,
+                            const double2* __restrict__ lam, const double2* __restrict__ un,
+                            const double2* __restrict__ un1, double theta, double* __restrict__ accD,
+                            double* __restrict__ accT) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_t) return;
+    const int4 qv = reinterpret_cast<const int4*>(tets)[t];
+    const int32_t v[4] = {qv.x, qv.y, qv.z, qv.w};
+    double X[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) X[k][c] = xyz[(int64_t)v[k] * 3 + c];
+    double E[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) E[r][c] = X[r + 1][c] - X[0][c];
+    const double c00 = E[1][1] * E[2][2] - E[1][2] * E[2][1];
+    const double c01 = E[1][2] * E[2][0] - E[1][0] * E[2][2];
+    const double c02 = E[1][0] * E[2][1] - E[1][1] * E[2][0];
+    const double det = E[0][0] * c00 + E[0][1] * c01 + E[0][2] * c02;
+    const double id = 1.0 / det;
+    double G[4][3];
+    G[1][0] = c00 * id; G[1][1] = c01 * id; G[1][2] = c02 * id;
+    G[2][0] = (E[0][2] * E[2][1] - E[0][1] * E[2][2]) * id;
+    G[2][1] = (E[0][0] * E[2][2] - E[0][2] * E[2][0]) * id;
+    G[2][2] = (E[0][1] * E[2][0] - E[0][0] * E[2][1]) * id;
+    G[3][0] = (E[0][1] * E[1][2] - E[0][2] * E[1][1]) * id;
+    G[3][1] = (E[0][2] * E[1][0] - E[0][0] * E[1][2]) * id;
+    G[3][2] = (E[0][0] * E[1][1] - E[0][1] * E[1][0]) * id;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) G[0][c] = -(G[1][c] + G[2][c] + G[3][c]);
+    const double vol = fabs(det) / 6.0;
+    const int f = comp[t];
+    double2 L[4], V[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int32_t d = dof_of[(int64_t)v[k] * nc + f];
+        L[k] = lam[d];
+        const double2 a0 = un[d], a1 = un1[d];
+        V[k] = make_double2(theta * a1.x + (1.0 - theta) * a0.x, theta * a1.y + (1.0 - theta) * a0.y);
+    }
+    // Re(L^T K V) and Re(L^T M V), unit coefficients
+    double sK = 0.0, sM = 0.0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const double re = L[r].x * V[c].x - L[r].y * V[c].y;
+            sK += vol * (G[r][0] * G[c][0] + G[r][1] * G[c][1] + G[r][2] * G[c][2]) * re;
+            sM += (r == c ? vol / 10.0 : vol / 20.0) * re;
+        }
+    accD[t] -= sK;
+    accT[t] -= sM;
+}
+
+__global__ void k_adj_facets(int64_t n_if, const int32_t* __restrict__ fcell, const int32_t* __restrict__ fface,
+                             const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                             const int32_t* __restrict__ nbr, const int32_t* __restrict__ comp,
+                             const int32_t* __restrict__ dof_of, int nc, const double2* __restrict__ lam,
+                             const double2* __restrict__ un, const double2* __restrict__ un1, double theta,
+                             double* __restrict__ accK) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_if) return;
+    const int32_t t = fcell[i];
+    const int fa = fface[i];
+    const int32_t nb = nbr[(int64_t)t * 4 + fa];
+    const int f = comp[t], g = comp[nb];
+    int32_t fv[3];
+    int m = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k != fa) fv[m++] = tets[(int64_t)t * 4 + k];
+    double P[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P[k][c] = xyz[(int64_t)fv[k] * 3 + c];
+    double e1[3], e2[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        e1[c] = P[1][c] - P[0][c];
+        e2[c] = P[2][c] - P[0][c];
+    }
+    const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                 cz = e1[0] * e2[1] - e1[1] * e2[0];
+    const double area = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+    double2 Lj[3], Vj[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int32_t da = dof_of[(int64_t)fv[k] * nc + f], db = dof_of[(int64_t)fv[k] * nc + g];
+        const double2 la = lam[da], lb = lam[db];
+        const double2 ua0 = un[da], ua1 = un1[da], ub0 = un[db], ub1 = un1[db];
+        Lj[k] = make_double2(la.x - lb.x, la.y - lb.y);
+        Vj[k] = make_double2(theta * (ua1.x - ub1.x) + (1.0 - theta) * (ua0.x - ub0.x),
+                             theta * (ua1.y - ub1.y) + (1.0 - theta) * (ua0.y - ub0.y));
+    }
+    double sK = 0.0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            sK += (r == c ? area / 6.0 : area / 12.0) * (Lj[r].x * Vj[c].x - Lj[r].y * Vj[c].y);
+    accK[i] -= sK;
+}
+
+}  // namespace
+
+void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const double* u0, double rtol,
+                  int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
+                  bt_stats* st) {
+    Mesh& m = ctx->mesh;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    BT_REQUIRE(!ctx->coeffs.has_cell_D, BT_ERR_STATE,
+               "bt_adjoint: gradients are defined for per-region isotropic D (clear the per-cell tensor)");
+    if (!ctx->s64) ctx->s64 = new Solver64();
+    Solver64& W = *ctx->s64;
+    prepare_fp64(ctx, W);
+    const int N = S.n_steps;
+    const double th = S.theta;
+    if (stride <= 0) stride = (int)std::ceil(std::sqrt((double)N));
+    stride = std::max(1, std::min(stride, N));
+    const int nck = (N + stride - 1) / stride;  // checkpoints u_0, u_stride, ...
+    DevBuf<double> d_u0;
+    if (u0) d_u0.upload(u0, m.n_v, s);
+    std::vector<double> hcn, hco, hout(kRed);
+    schedule_row(S, seq, q, hcn, hco);
+    // adjoint schedule: step j builds lambda_{N-j} with A_{N-j-1} and B_{N-j}
+    std::vector<double> acn(N), aco(N, 0.0);
+    for (int j = 0; j < N; ++j) {
+        acn[j] = hcn[N - 1 - j];
+        if (j >= 1) aco[j] = hco[N - j];
+    }
+    DevBuf<double> d_cn, d_co, d_acn, d_aco;
+    d_cn.upload(hcn.data(), N, s);
+    d_co.upload(hco.data(), N, s);
+    d_acn.upload(acn.data(), N, s);
+    d_aco.upload(aco.data(), N, s);
+    pack_signal_fp64(ctx, W, gdir, u0 ? d_u0.p : nullptr);
+    const size_t vb = (size_t)W.n_pad * sizeof(double2);
+    DevBuf<double2> ck, seg, lam;
+    ck.alloc((size_t)(nck + 1) * W.n_pad);
+    seg.alloc((size_t)(stride + 1) * W.n_pad);
+    lam.alloc(W.n_pad);
+    DevBuf<double> accD, accT, accK;
+    accD.alloc(m.n_t);
+    accD.zero(s);
+    accT.alloc(m.n_t);
+    accT.zero(s);
+    accK.alloc(std::max<int64_t>(1, m.n_iface));
+    accK.zero(s);
+    std::vector<int32_t> hit;
+    int64_t total_iters = 0;
+    int32_t max_iters = 0;
+    auto count = [&](const std::vector<int32_t>& v) {
+        for (int32_t x : v) {
+            total_iters += x;
+            max_iters = std::max(max_iters, x);
+        }
+    };
+    float ms = 0.0f;
+    BT_CUDA(cudaEventRecord(ctx->ev0, s));
+    // forward: checkpoints ck[0] = u_0, ck[j] = u_{j*stride}
+    BT_CUDA(cudaMemcpyAsync(ck.p, W.u[0].p, vb, cudaMemcpyDeviceToDevice, s));
+    ms += run_steps_fp64(ctx, W, d_cn, d_co, N, ctx->opt_fp64_extrapolate != 0, nullptr, ck.p + W.n_pad, stride,
+                         rtol, maxit, &hit, nullptr, hout.data());
+    count(hit);
+    *sig = hout[0];
+    // lambda_N = A_{N-1}^{-1} w  (x0 = 0)
+    W.u[0].zero(s);
+    W.u[2].zero(s);
+    ms += run_steps_fp64(ctx, W, d_acn.p, d_aco.p, 1, false, W.w, nullptr, 1, rtol, maxit, &hit, nullptr,
+                         nullptr);
+    count(hit);
+    BT_CUDA(cudaMemcpyAsync(lam.p, W.u[1].p, vb, cudaMemcpyDeviceToDevice, s));
+    const unsigned cb = (unsigned)((m.n_t + 127) / 128), fb = (unsigned)((m.n_iface + 127) / 128);
+    for (int sg = nck - 1; sg >= 0; --sg) {
+        const int a0 = sg * stride, b0 = std::min(a0 + stride, N);
+        // recompute u_{a0..b0} from the checkpoint (no extrapolation at the restart)
+        BT_CUDA(cudaMemcpyAsync(seg.p, ck.p + (size_t)sg * W.n_pad, vb, cudaMemcpyDeviceToDevice, s));
+        BT_CUDA(cudaMemcpyAsync(W.u[0].p, seg.p, vb, cudaMemcpyDeviceToDevice, s));
+        BT_CUDA(cudaMemcpyAsync(W.u[2].p, seg.p, vb, cudaMemcpyDeviceToDevice, s));
+        ms += run_steps_fp64(ctx, W, d_cn.p + a0, d_co.p + a0, b0 - a0, ctx->opt_fp64_extrapolate != 0, nullptr,
+                             seg.p + W.n_pad, 1, rtol, maxit, &hit, nullptr, nullptr);
+        count(hit);
+        for (int n = b0 - 1; n >= a0; --n) {
+            const double2* un = seg.p + (size_t)(n - a0) * W.n_pad;
+            const double2* un1 = seg.p + (size_t)(n - a0 + 1) * W.n_pad;
+            k_adj_cells<<<cb, 128, 0, s>>>(m.n_t, m.xyz, m.tets, m.comp, m.dof_of, m.n_comp, lam.p, un, un1, th,
+                                           accD.p, accT.p);
+            if (m.n_iface > 0)
+                k_adj_facets<<<fb, 128, 0, s>>>(m.n_iface, m.iface_cell, m.iface_face, m.xyz, m.tets, m.nbr,
+                                                m.comp, m.dof_of, m.n_comp, lam.p, un, un1, th, accK.p);
+            BT_CUDA(cudaGetLastError());
+            if (n >= 1) {  // lambda_n = A_{n-1}^{-1} B_n lambda_{n+1}
+                const int j = N - n;
+                BT_CUDA(cudaMemcpyAsync(W.u[0].p, lam.p, vb, cudaMemcpyDeviceToDevice, s));
+                BT_CUDA(cudaMemcpyAsync(W.u[2].p, lam.p, vb, cudaMemcpyDeviceToDevice, s));
+                ms += run_steps_fp64(ctx, W, d_acn.p + j, d_aco.p + j, 1, false, nullptr, nullptr, 1, rtol, maxit,
+                                     &hit, nullptr, nullptr);
+                count(hit);
+                BT_CUDA(cudaMemcpyAsync(lam.p, W.u[1].p, vb, cudaMemcpyDeviceToDevice, s));
+            }
+        }
+    }
+    // reduce once, in index order
+    std::vector<double> hD(m.n_t), hT(m.n_t), hK(m.n_iface);
+    std::vector<int32_t> hreg(m.n_t), hfc(m.n_iface), hff(m.n_iface), hnb(m.n_t * 4);
+    accD.download(hD.data(), m.n_t, s);
+    accT.download(hT.data(), m.n_t, s);
+    if (m.n_iface > 0) {
+        accK.download(hK.data(), m.n_iface, s);
+        m.iface_cell.download(hfc.data(), m.n_iface, s);
+        m.iface_face.download(hff.data(), m.n_iface, s);
+    }
+    m.region.download(hreg.data(), m.n_t, s);
+    m.nbr.download(hnb.data(), m.n_t * 4, s);
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    BT_CUDA(cudaStreamSynchronize(s));
+    const int nr = m.n_regions;
+    for (int r = 0; r < nr; ++r) {
+        if (dD) dD[r] = 0.0;
+        if (dinvT2) dinvT2[r] = 0.0;
+    }
+    if (dkappa)
+        for (int k = 0; k < nr * nr; ++k) dkappa[k] = 0.0;
+    for (int64_t t = 0; t < m.n_t; ++t) {
+        if (dD) dD[hreg[t]] += hD[t];
+        if (dinvT2) dinvT2[hreg[t]] += hT[t];
+    }
+    if (dkappa) {
+        std::vector<double> pair((size_t)nr * nr, 0.0);
+        for (int64_t i = 0; i < m.n_iface; ++i) {
+            const int32_t t = hfc[i];
+            const int32_t nb = hnb[(size_t)t * 4 + hff[i]];
+            const int r1 = std::min(hreg[t], hreg[nb]), r2 = std::max(hreg[t], hreg[nb]);
+            pair[(size_t)r1 * nr + r2] += hK[i];
+        }
+        for (int r1 = 0; r1 < nr; ++r1)
+            for (int r2 = r1; r2 < nr; ++r2) {
+                dkappa[(size_t)r1 * nr + r2] = pair[(size_t)r1 * nr + r2];
+                dkappa[(size_t)r2 * nr + r1] = pair[(size_t)r1 * nr + r2];
+            }
+    }
+    float total = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&total, ctx->ev0, ctx->ev2));
+    if (st) {
+        st->steps = N;
+        st->max_iterations = max_iters;
+        st->total_iterations = total_iters;
+        st->max_rel_residual = rtol;
+        st->refinements = 0;
+        st->graph_launches = 0;
+        st->kernel_launches = 0;
+        st->gpu_ms = total;
+        st->stepper_ms = ms;
+    }
 }
 
 }  // namespace bt

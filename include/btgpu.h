@@ -150,6 +150,21 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
              double rtol, int32_t max_iterations, double* signal_out,
              double* compartment_out, double* S0_out, bt_stats* stats);
 
+/* Discrete adjoint of the FP64 solve of one signal: the signal and its
+ * derivatives with respect to the per-region isotropic D (dS_dD[n_regions]),
+ * 1/T2 (dS_dinvT2[n_regions]) and the permeability of each region pair
+ * (dS_dkappa[n_regions*n_regions], symmetric: both entries of a pair hold the
+ * derivative with respect to that pair's single value).  Derivatives are of
+ * the unnormalised signal int Re(u(T)) dx; divide by S0 for the normalised
+ * one.  Forward states are recomputed from checkpoints every
+ * checkpoint_stride steps (0: ceil(sqrt(n_steps))).  The reference has no
+ * adjoint; its gradients would be finite differences of MRI_simulation.solve
+ * (DmriFemLib.py:878-915).  Any output pointer may be NULL. */
+int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0,
+               double rtol, int32_t max_iterations, int32_t checkpoint_stride,
+               double* signal_out, double* dS_dD, double* dS_dinvT2, double* dS_dkappa,
+               bt_stats* stats);
+
 /* Tuning knobs (no counterpart in the reference).  Keys:
  *   "mixed.lanes_per_row"   1,2,4,...,32 (0: autotune, the default)
  *   "mixed.blocks_per_sm"   co-resident blocks of the batched kernel (0: autotune)

@@ -1,0 +1,117 @@
+"""GPU: discrete-adjoint gradients of the FP64 solve (bt_adjoint) against
+central finite differences with a 1e-6 relative step, of the GPU forward and of
+the CPU oracle.  Tolerance: 1e-5 relative to the gradient's scale."""
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+ADJ_RTOL = 1e-5
+
+
+def layered_case(pkg, n=8):
+    xyz, tets = pkg.meshgen.kuhn_box(-12, 12, n)
+    reg = pkg.meshgen.layered_sphere_regions(xyz, tets, [4.0, 7.0, 10.0])
+    D = np.array([1e-3, 2e-3, 3e-3, 3e-3])
+    invT2 = 1.0 / np.array([5e4, 8e4, 1e5, np.inf])
+    kp = np.zeros((4, 4))
+    for (i, j), v in {(0, 1): 1e-5, (1, 2): 3e-5, (2, 3): 5e-5}.items():
+        kp[i, j] = kp[j, i] = v
+    return xyz, tets, reg, D, invT2, kp
+
+
+def make(pkg, xyz, tets, reg, D, invT2, kp):
+    ctx = pkg.Context(0)
+    ctx.mesh_upload(xyz, tets, reg, 4)
+    ctx.set_coefficients(D, invT2, kp)
+    ctx.assemble()
+    p = pkg.sequences.pgse(10600, 43100)
+    fn, fo = pkg.sequences.profile_samples(p, 200.0)
+    ctx.set_schedule(fn, fo, 200.0)
+    return ctx, pkg.sequences.b_to_q(3000.0, p.int4gb())
+
+
+G = np.array([0.3, 0.8, 0.52])
+G = G / np.linalg.norm(G)
+
+
+def signal(ctx, q, D, invT2, kp):
+    ctx.set_coefficients(D, invT2, kp)
+    ctx.assemble()
+    return ctx.solve([q], G, rtol=1e-14, max_iterations=20000)["signal"][0]
+
+
+def test_adjoint_matches_finite_differences(pkg, lib):
+    xyz, tets, reg, D, invT2, kp = layered_case(pkg)
+    ctx, q = make(pkg, xyz, tets, reg, D, invT2, kp)
+    adj = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000)
+    base = signal(ctx, q, D, invT2, kp)
+    assert abs(adj["signal"] - base) <= 1e-10 * abs(base)
+    h = 1e-6
+    scale = {"D": np.max(np.abs(adj["dD"] * D)), "T": np.max(np.abs(adj["dinvT2"] * invT2)),
+             "K": max(abs(adj["dkappa"][i, j] * kp[i, j]) for i, j in ((0, 1), (1, 2), (2, 3)))}
+    for r in range(4):
+        Dp, Dm = D.copy(), D.copy()
+        Dp[r] *= 1 + h
+        Dm[r] *= 1 - h
+        fd = (signal(ctx, q, Dp, invT2, kp) - signal(ctx, q, Dm, invT2, kp)) / (2 * h * D[r])
+        assert abs(adj["dD"][r] - fd) * D[r] <= ADJ_RTOL * scale["D"], ("D", r, adj["dD"][r], fd)
+    for r in range(3):                       # region 3 has no T2 decay (1/T2 = 0)
+        Tp, Tm = invT2.copy(), invT2.copy()
+        Tp[r] *= 1 + h
+        Tm[r] *= 1 - h
+        fd = (signal(ctx, q, D, Tp, kp) - signal(ctx, q, D, Tm, kp)) / (2 * h * invT2[r])
+        assert abs(adj["dinvT2"][r] - fd) * invT2[r] <= ADJ_RTOL * scale["T"], ("T2", r, adj["dinvT2"][r], fd)
+    for i, j in ((0, 1), (1, 2), (2, 3)):
+        Kp, Km = kp.copy(), kp.copy()
+        Kp[i, j] = Kp[j, i] = kp[i, j] * (1 + h)
+        Km[i, j] = Km[j, i] = kp[i, j] * (1 - h)
+        fd = (signal(ctx, q, D, invT2, Kp) - signal(ctx, q, D, invT2, Km)) / (2 * h * kp[i, j])
+        assert abs(adj["dkappa"][i, j] - fd) * kp[i, j] <= ADJ_RTOL * scale["K"], ("kappa", i, j)
+        assert adj["dkappa"][i, j] == adj["dkappa"][j, i]
+    assert np.all(adj["dkappa"][[0, 0, 1], [2, 3, 3]] == 0.0)     # no interface between these regions
+    ctx.close()
+
+
+def test_adjoint_matches_oracle_fd(pkg, lib):
+    """One gradient against the CPU oracle's central difference (SuperLU)."""
+    xyz, tets, reg, D, invT2, kp = layered_case(pkg, n=6)
+    ctx, q = make(pkg, xyz, tets, reg, D, invT2, kp)
+    adj = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000)
+    h = 1e-6
+    vals = []
+    for sgn in (1, -1):
+        Kx = kp.copy()
+        Kx[1, 2] = Kx[2, 1] = kp[1, 2] * (1 + sgn * h)
+        sd = oracle.duplicated_system(xyz, tets, reg, D, invT2, Kx)
+        vals.append(oracle.solve_duplicated(sd, oracle.PGSE(10600, 43100), q, G, 200.0).signal)
+    fd = (vals[0] - vals[1]) / (2 * h * kp[1, 2])
+    assert abs(adj["dkappa"][1, 2] - fd) <= ADJ_RTOL * abs(fd)
+    ctx.close()
+
+
+def test_checkpoint_stride_invariance_and_autograd(pkg, lib):
+    import torch
+    xyz, tets, reg, D, invT2, kp = layered_case(pkg, n=6)
+    ctx, q = make(pkg, xyz, tets, reg, D, invT2, kp)
+    a = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000, stride=1)
+    b = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000, stride=0)
+    c = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000, stride=270)
+    for k in ("dD", "dinvT2", "dkappa"):
+        ref = np.max(np.abs(a[k]))
+        assert np.max(np.abs(a[k] - b[k])) <= 1e-9 * ref and np.max(np.abs(a[k] - c[k])) <= 1e-9 * ref
+    from importlib import import_module
+    ag = import_module(pkg.__name__ + ".autograd")
+    Dt = torch.tensor(D, requires_grad=True)
+    Tt = torch.tensor(invT2, requires_grad=True)
+    Kt = torch.tensor(kp, requires_grad=True)
+    s = ag.BlochTorreySignal.apply(Dt, Tt, Kt, ctx, q, G, 0)
+    s.backward()
+    S0 = ctx.info()["volume"]
+    assert abs(float(s.detach()) - a["signal"] / S0) <= 1e-12
+    assert np.allclose(Dt.grad.numpy(), a["dD"] / S0, rtol=1e-9, atol=0)
+    assert np.allclose(Kt.grad.numpy(), a["dkappa"] / S0, rtol=1e-9, atol=0)
+    ctx.close()
