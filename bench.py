@@ -185,6 +185,7 @@ def gpu_run(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     pkg = importlib.import_module(PKG)
+    replicas = importlib.import_module(PKG + ".replicas")
     pkg._native.load(pkg.build())
     w = pkg.meshgen.workload(args.workload)
     prof = w["profiles"]
@@ -234,11 +235,7 @@ def gpu_run(args):
             torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
-        tot = sum(a.elapsed_time(b) for a, b in evs)
-        if world > 1:
-            t = torch.tensor([tot], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            tot = float(t.item())
+        tot = replicas.max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), device="cuda")
         return tot, outs, clk.summary()
 
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
