@@ -71,14 +71,16 @@ def alg_bytes_mixed(n, nnz, nsig, steps, iters, sweeps):
     Each signal is two FP32 complex slots (Re / Im right-hand sides, 8 bytes a
     value).  per inner iteration and signal-dof: 2 slots x (gather z 8 + p,q in
     16 + p,q out 16 + p,q,d,r in 32 + d,r,z out 24) = 192 B, plus the matrix
-    nnz*(4 + 16) once per iteration for the whole batch; per refinement sweep
-    and signal-dof: gather d 16, u and r in/out as double-float 64, restart of
-    the five slot vectors 80 = 160 B, matrix nnz*(4 + 32); per time step and
-    signal-dof: gather u 16, r out 16, slot vectors 80 = 112 B, matrix
-    nnz*(4 + 8 + 32).
+    nnz*(4 + 16) once per iteration for the whole batch.  Per time step and
+    signal-dof: residual at u_n (gather u 16, r out 16) + extrapolated-guess
+    correction (gather two history vectors 16, r in/out 32, u in 8, history out
+    8, restart of the five slot vectors 80) = 176 B, matrix nnz*(4 + 8 + 32) +
+    nnz*(4 + 32).  Per refinement sweep and signal-dof: gather d 16, u and r
+    in/out as double-float 64, history in/out 16, restart 80 = 176 B, matrix
+    nnz*(4 + 32).
     """
-    return (iters * (192 * n * nsig + 20 * nnz) + sweeps * (160 * n * nsig + 36 * nnz)
-            + steps * (112 * n * nsig + 44 * nnz))
+    return (iters * (192 * n * nsig + 20 * nnz) + sweeps * (176 * n * nsig + 36 * nnz)
+            + steps * (176 * n * nsig + 80 * nnz))
 
 
 class ClockSampler:

@@ -295,9 +295,11 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
             BT_REQUIRE(iv == 0 || iv == 1 || iv == 2 || iv == 4 || iv == 8 || iv == 16 || iv == 32, BT_ERR_INVALID,
                        "mixed.lanes_per_row must be 0 or a power of two <= 32");
             ctx->opt_mixed_lpr = iv > 0 ? iv : -1;
+            bt::reset_tuning_mixed(ctx);
         } else if (k == "mixed.blocks_per_sm") {
             BT_REQUIRE(iv >= 0 && iv <= 8, BT_ERR_INVALID, "mixed.blocks_per_sm must be in [0, 8]");
             ctx->opt_mixed_blocks_per_sm = iv > 0 ? iv : -1;
+            bt::reset_tuning_mixed(ctx);
         } else if (k == "mixed.max_sweeps") {
             BT_REQUIRE(iv >= 1 && iv <= 64, BT_ERR_INVALID, "mixed.max_sweeps must be in [1, 64]");
             ctx->opt_mixed_max_sweeps = iv;
@@ -307,6 +309,13 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
         } else if (k == "mixed.eps_next") {
             BT_REQUIRE(value > 0.0 && value < 1.0, BT_ERR_INVALID, "mixed.eps_next must be in (0, 1)");
             ctx->opt_mixed_eps_next = value;
+        } else if (k == "mixed.blocked_rows") {
+            BT_REQUIRE(iv >= -1 && iv <= 1, BT_ERR_INVALID, "mixed.blocked_rows must be -1 (tune), 0 or 1");
+            ctx->opt_mixed_blocked = iv;
+            bt::reset_tuning_mixed(ctx);
+        } else if (k == "mixed.extrapolate") {
+            BT_REQUIRE(iv >= 0 && iv <= 2, BT_ERR_INVALID, "mixed.extrapolate must be 0, 1 or 2");
+            ctx->opt_mixed_extrapolate = iv;
         } else if (k == "fp64.extrapolate") {
             ctx->opt_fp64_extrapolate = iv ? 1 : 0;
         } else {

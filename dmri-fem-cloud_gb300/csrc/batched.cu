@@ -62,6 +62,7 @@ struct SolverMixed {
     DevBuf<double> w;         // per row signal weight
     DevBuf<int32_t> rcomp;
     DevBuf<float2> uh, ul, rh, rl, d0, d1, ri, z, p, q;  // [n][Rp]
+    DevBuf<float2> h0, h1, h2;   // per signal [n][Rp/2]: total corrections of the last three steps
     DevBuf<float2> partials, fin;   // double-float (hi, lo) sums
     DevBuf<double> sigpart;      // [warps][64][1+kMaxCompartments]
     DevBuf<unsigned> bar;
@@ -77,7 +78,10 @@ struct SolverMixed {
     // final solutions of the last solve: [nsig][n] complex (hi + lo, as double2)
     std::vector<double2> saved;
     int32_t saved_nsig = 0;
-    std::map<std::pair<int64_t, int32_t>, std::pair<int, int>> tuned;  // (n,Rp) -> (LPR, blocks/SM)
+    struct Geo {
+        int lpr, per_sm, blocked;
+    };
+    std::map<std::pair<int64_t, int32_t>, Geo> tuned;  // (n, R) -> launch geometry
 };
 
 struct MixArgs {
@@ -101,6 +105,8 @@ struct MixArgs {
     float4* z;
     float4* p;
     float4* q;
+    float2* hist[3];      // per signal: u_{m+1} - u_m of steps m = s-2, s-1, s (rotating by s % 3)
+    int32_t extrap;       // initial guess: 0 u_n, 1 linear, 2 quadratic extrapolation in time
     float2* partials;
     float2* fin;
     double* sigpart;
@@ -121,6 +127,7 @@ struct MixArgs {
     float eps_first;
     float eps_next;
     int32_t two_stage;
+    int32_t blocked;      // rows: 0 interleaved over all warps, 1 contiguous range per block
     int32_t* iters;
     int32_t* sweeps;
     double* sig;  // [Rp][1+kMaxCompartments]
@@ -187,6 +194,12 @@ __device__ __forceinline__ float2 cdivf(float2 a, float2 b) {
     return make_float2(fmaf(a.x, r, a.y) / d, fmaf(a.y, r, -a.x) / d);
 }
 __device__ __forceinline__ float2 cinvf(float2 b) { return cdivf(make_float2(1.0f, 0.0f), b); }
+// Offset of the extrapolated initial guess from u_n: c1 (u_n - u_{n-1}) + c2 (u_{n-1} - u_{n-2}).
+// The same FP32 expression is used wherever the offset is formed, so the state
+// and the residual see bitwise the same offset.
+__device__ __forceinline__ float2 guess_offset(float2 h1, float2 h2, float c1, float c2) {
+    return make_float2(fmaf(c2, h2.x, c1 * h1.x), fmaf(c2, h2.y, c1 * h1.y));
+}
 __device__ __forceinline__ bool cnonzero(float2 v) {
     return (v.x != 0.0f || v.y != 0.0f) && isfinite(v.x) && isfinite(v.y);
 }
@@ -259,15 +272,24 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
             if ((int)((blockIdx.x * kWarpsB + wb) % nchunks) == c) s = dfa(s, smem[(wb * C + o) * kNV + k]);
         a.partials[(size_t)blockIdx.x * a.Rp * kNV + t] = s;
     }
-    if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
     const int V = a.Rp * kNV;
     if (a.two_stage) {
+        if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
         // stage 2: one warp per value; lane l adds blocks l, l+32, ... and the
         // warp combines the 32 lane sums in a fixed butterfly (lane 0's order)
         const int gw = blockIdx.x * kWarpsB + wib;
         for (int t = gw; t < V; t += nb * kWarpsB) {
             float2 s = make_float2(0.f, 0.f);
-            for (unsigned b = lane; b < nb; b += 32) s = dfa(s, __ldcg(&a.partials[(size_t)b * V + t]));
+            for (unsigned b0 = lane; b0 < nb; b0 += 4u * 32u) {
+                float2 tv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const unsigned b = b0 + 32u * u;
+                    tv[u] = (b < nb) ? __ldcg(&a.partials[(size_t)b * V + t]) : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) s = dfa(s, tv[u]);
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1)
                 s = dfa(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
@@ -282,22 +304,69 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
                 out[j][k] = f.x + f.y;
             }
     } else {
-        // one stage: each block sums all partials (few values) into shared
-        // memory; G lanes per value stride over the blocks and combine in a
-        // fixed butterfly, so every block forms bitwise the same sums
-        __syncthreads();
-        int G = 32;
-        while (G > 1 && V * G > (int)blockDim.x) G >>= 1;
-        const int part = threadIdx.x % G;
-        for (int t0 = 0; t0 < V; t0 += blockDim.x / G) {
-            const int t = t0 + threadIdx.x / G;
-            float2 s = make_float2(0.f, 0.f);
-            if (t < V)
-                for (unsigned b = part; b < nb; b += G) s = dfa(s, __ldcg(&a.partials[(size_t)b * V + t]));
-            for (int o = G / 2; o > 0; o >>= 1)
-                s = dfa(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
-            if (part == 0 && t < V) smem[t] = s;
+        // one stage: the last block to arrive sums all partials (G lanes per value
+        // stride over the blocks and combine in a fixed butterfly, so the sums do not
+        // depend on which block is last), publishes them in fin and releases the
+        // others, which read only the V sums
+        __shared__ int s_last, s_ok;
+        const unsigned target = gen + 1;
+        if (threadIdx.x == 0) {
+            // no status check before arriving (it would cost a round trip): a block
+            // that left on an error never arrives, and the waiters below see the
+            // status within 256 polls
+            s_ok = 1;
+            s_last = (atom_add_acqrel_u32(&a.bar[0], 1u) == nb - 1);
         }
+        __syncthreads();
+        if (s_last) {
+            int G = 32;
+            while (G > 1 && V * G > (int)blockDim.x) G >>= 1;
+            const int part = threadIdx.x % G;
+            for (int t0 = 0; t0 < V; t0 += blockDim.x / G) {
+                const int t = t0 + threadIdx.x / G;
+                float2 s = make_float2(0.f, 0.f);
+                if (t < V)
+                    for (unsigned b0 = part; b0 < nb; b0 += 8u * G) {
+                        float2 tv[8];   // eight independent loads in flight; zero padding adds exactly nothing
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const unsigned b = b0 + (unsigned)G * u;
+                            tv[u] = (b < nb) ? __ldcg(&a.partials[(size_t)b * V + t]) : make_float2(0.f, 0.f);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) s = dfa(s, tv[u]);
+                    }
+                for (int o = G / 2; o > 0; o >>= 1)
+                    s = dfa(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
+                if (part == 0 && t < V) {
+                    smem[t] = s;
+                    __stcg(&a.fin[t], s);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                a.bar[0] = 0;
+                st_release_u32(&a.bar[1], target);
+            }
+        } else {
+            if (threadIdx.x == 0) {
+                const unsigned long long t0 = globaltimer_ns();
+                unsigned spins = 0;
+                while (ld_acquire_u32(&a.bar[1]) != target) {
+                    if (++spins > kBarrierMaxSpins || (spins & 255u) == 0u &&
+                        (globaltimer_ns() - t0 > kBarrierTimeoutNs || ld_relaxed_i32(a.status) != DEV_OK)) {
+                        atomicCAS(a.status, DEV_OK, DEV_TIMEOUT);
+                        s_ok = 0;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            __syncthreads();
+            if (!s_ok) return false;
+            for (int t = threadIdx.x; t < V; t += blockDim.x) smem[t] = __ldcg(&a.fin[t]);
+        }
+        gen = target;
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < 2; ++j)
@@ -310,7 +379,7 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
 
 // ------------------------------------------------------------------ kernel ----
 template <int LPR>
-__global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
+__global__ void __maxnreg__(120) k_batched(MixArgs a) {
     constexpr int G = 32 / LPR;  // rows per warp-unit
     constexpr int C = 2 * LPR;   // RHS per warp-unit
     __shared__ float2 smem[kWarpsB * 64 * kNV > kMaxRhs * kNV ? kWarpsB * 64 * kNV : kMaxRhs * kNV];
@@ -326,7 +395,19 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
     const int c4 = r0 >> 1;                        // float4 index of the lane's 2 RHS inside a row
     const int Rp4 = a.Rp >> 1;                     // float4 per row
     const int ngroups = (a.n + G - 1) / G;
-    const int g0 = gw / nchunks, gstride = total_warps / nchunks;
+    // Row groups of this warp.  Interleaved: consecutive groups go to consecutive
+    // warps of the whole grid.  Blocked: each block owns a contiguous range of
+    // groups, so the neighbour rows its warps gather overlap and are reused in L1.
+    int g0, gend, gstride;
+    if (a.blocked) {
+        g0 = (int)(((long long)ngroups * blockIdx.x) / nb) + (threadIdx.x >> 5) / nchunks;
+        gend = (int)(((long long)ngroups * (blockIdx.x + 1)) / nb);
+        gstride = kWarpsB / nchunks;
+    } else {
+        g0 = gw / nchunks;
+        gend = ngroups;
+        gstride = total_warps / nchunks;
+    }
     unsigned gen = 0;
     // per-lane RHS parameters
     double qd[2];
@@ -361,39 +442,46 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
             cn[j] = (float)(a.theta * qd[j] * fnv);
             cs[j] = (float)(a.theta * qd[j] * fnv + (1.0 - a.theta) * qd[j] * fov);  // cn + co
         }
-        // ---- phase S: r = -(S u + i (cn+co) Jg u) in double-float for the lane's
-        //      signal; the FP32 inner solve starts from Re(r) (slot 0) and Im(r) (slot 1)
-        KF red[2][kNV];
-#pragma unroll
-        for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int k = 0; k < kNV; ++k) red[j][k] = KF{0.0f, 0.0f};
-        for (int g = g0; g < ngroups; g += gstride) {
+        // ---- phase S, pass 1: r = -(S u + i (cn+co) Jg u) = b - A u_n in double-float
+        //      for the lane's signal
+        for (int g = g0; g < gend; g += gstride) {
             const int row = g * G + slot;
             if (row >= a.n) continue;
             DF sr[2], jx[2], jy[2], jz[2];  // [re/im]
 #pragma unroll
             for (int c = 0; c < 2; ++c) sr[c] = jx[c] = jy[c] = jz[c] = DF{0.0f, 0.0f};
             const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
-            for (int e = e0; e < e1; ++e) {
-                const int cidx = a.col[e];
-                const float2 s2 = a.mS[e];
-                const float4 hi = a.mA[e], lo = a.mL[e];
-                const float2 uh = a.uh[(size_t)cidx * Rp4 + c4];
-                const float2 ul = a.ul[(size_t)cidx * Rp4 + c4];
-                const float uhv[2] = {uh.x, uh.y}, ulv[2] = {ul.x, ul.y};
+            for (int e = e0; e < e1; e += 4) {   // four gathers in flight, predicated tail
+                int cc[4];
+                float2 s2[4], uh[4], ul[4];
+                float4 hi[4], lo[4];
+                const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    df_fma(sr[c], s2.x, s2.y, uhv[c], ulv[c]);
-                    df_fma(jx[c], hi.y, lo.y, uhv[c], ulv[c]);
-                    df_fma(jy[c], hi.z, lo.z, uhv[c], ulv[c]);
-                    df_fma(jz[c], hi.w, lo.w, uhv[c], ulv[c]);
+                for (int u = 0; u < 4; ++u) {
+                    const bool ok = e + u < e1;
+                    cc[u] = ok ? a.col[e + u] : row;
+                    s2[u] = ok ? a.mS[e + u] : make_float2(0.f, 0.f);
+                    hi[u] = ok ? a.mA[e + u] : z4;
+                    lo[u] = ok ? a.mL[e + u] : z4;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    uh[u] = a.uh[(size_t)cc[u] * Rp4 + c4];
+                    ul[u] = a.ul[(size_t)cc[u] * Rp4 + c4];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float uhv[2] = {uh[u].x, uh[u].y}, ulv[2] = {ul[u].x, ul[u].y};
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        df_fma(sr[c], s2[u].x, s2[u].y, uhv[c], ulv[c]);
+                        df_fma(jx[c], hi[u].y, lo[u].y, uhv[c], ulv[c]);
+                        df_fma(jy[c], hi[u].z, lo[u].z, uhv[c], ulv[c]);
+                        df_fma(jz[c], hi[u].w, lo[u].w, uhv[c], ulv[c]);
+                    }
                 }
             }
-            const float4 dgr = a.dg[row];
-            const float wr = (float)a.w[row] * a.inv_k;
             const size_t vi = (size_t)row * Rp4 + c4;
-            const float2 uhr = a.uh[vi];
             DF jg[2];
 #pragma unroll
             for (int c = 0; c < 2; ++c)
@@ -404,6 +492,82 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
             const DF im = df_add(df_neg(df_norm(sr[1])), df_scale(jg[0], -cs[0]));
             a.rh[vi] = make_float2(re.h, im.h);
             a.rl[vi] = make_float2(re.l, im.l);
+        }
+        // ---- phase S, pass 2 (same rows, same threads: no barrier): start from the
+        //      extrapolated guess u_n + e, r -= A e in double-float; the FP32 inner solve
+        //      starts from Re(r) (slot 0) and Im(r) (slot 1).  u itself is not written
+        //      here (other threads may still gather u_n in pass 1): e is kept in the
+        //      history slot of this step and added to u by the first phase U.
+        const float c1 = (a.extrap == 0 || step == 0) ? 0.f : ((a.extrap == 1 || step == 1) ? 1.f : 2.f);
+        const float c2 = (a.extrap == 2 && step >= 2) ? -1.f : 0.f;
+        const float2* __restrict__ H1 = a.hist[(step + 2) % 3];
+        const float2* __restrict__ H2 = a.hist[(step + 1) % 3];
+        float2* const Hc = a.hist[step % 3];
+        KF red[2][kNV];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV; ++k) red[j][k] = KF{0.0f, 0.0f};
+        for (int g = g0; g < gend; g += gstride) {
+            const int row = g * G + slot;
+            if (row >= a.n) continue;
+            const size_t vi = (size_t)row * Rp4 + c4;
+            DF ar[2], jx[2], jy[2], jz[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) ar[c] = jx[c] = jy[c] = jz[c] = DF{0.0f, 0.0f};
+            float2 ev = make_float2(0.f, 0.f);
+            if (c1 != 0.0f) {   // uniform over the grid
+                const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
+                for (int e = e0; e < e1; e += 4) {   // four gathers in flight, predicated tail
+                    int cc[4];
+                    float4 hi[4], lo[4];
+                    float2 h1[4], h2[4];
+                    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const bool ok = e + u < e1;
+                        cc[u] = ok ? a.col[e + u] : row;
+                        hi[u] = ok ? a.mA[e + u] : z4;
+                        lo[u] = ok ? a.mL[e + u] : z4;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const size_t ni = (size_t)cc[u] * Rp4 + c4;
+                        h1[u] = H1[ni];
+                        h2[u] = H2[ni];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float2 en = guess_offset(h1[u], h2[u], c1, c2);
+                        const float ec[2] = {en.x, en.y};
+#pragma unroll
+                        for (int c = 0; c < 2; ++c) {
+                            df_fma(ar[c], hi[u].x, lo[u].x, ec[c], 0.0f);
+                            df_fma(jx[c], hi[u].y, lo[u].y, ec[c], 0.0f);
+                            df_fma(jy[c], hi[u].z, lo[u].z, ec[c], 0.0f);
+                            df_fma(jz[c], hi[u].w, lo[u].w, ec[c], 0.0f);
+                        }
+                    }
+                }
+                ev = guess_offset(H1[vi], H2[vi], c1, c2);
+            }
+            DF jg[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+                jg[c] = df_add(df_add(df_scale(df_norm(jx[c]), gx[0]), df_scale(df_norm(jy[c]), gy[0])),
+                               df_scale(df_norm(jz[c]), gz[0]));
+            // A e = A_re e + i cn Jg e
+            const DF aer = df_add(df_norm(ar[0]), df_scale(jg[1], -cn[0]));
+            const DF aei = df_add(df_norm(ar[1]), df_scale(jg[0], cn[0]));
+            const float2 rh0 = a.rh[vi], rl0 = a.rl[vi];
+            const DF re = df_add(DF{rh0.x, rl0.x}, df_neg(aer));
+            const DF im = df_add(DF{rh0.y, rl0.y}, df_neg(aei));
+            const float2 uhr = a.uh[vi];
+            a.rh[vi] = make_float2(re.h, im.h);
+            a.rl[vi] = make_float2(re.l, im.l);
+            Hc[vi] = ev;
+            const float4 dgr = a.dg[row];
+            const float wr = (float)a.w[row] * a.inv_k;
             const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
             const float2 z0 = make_float2(dinv.x * re.h, dinv.y * re.h);
             const float2 z1 = make_float2(dinv.x * im.h, dinv.y * im.h);
@@ -470,7 +634,7 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                 for (int j = 0; j < 2; ++j)
 #pragma unroll
                     for (int k = 0; k < kNV; ++k) mu[j][k] = KF{0.0f, 0.0f};
-                for (int g = g0; g < ngroups; g += gstride) {
+                for (int g = g0; g < gend; g += gstride) {
                     const int row = g * G + slot;
                     if (row >= a.n) continue;
                     float2 sA[2], sx[2], sy[2], sz[2];
@@ -487,24 +651,25 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                             sz[j].x = fmaf(m.w, zj[j].x, sz[j].x); sz[j].y = fmaf(m.w, zj[j].y, sz[j].y);
                         }
                     };
-                    int e = e0;
-                    // four independent neighbour gathers in flight per warp
-                    for (; e + 4 <= e1; e += 4) {
-                        int cc[4];
-                        float4 mm[4], zz[4];
+                    const size_t vi = (size_t)row * Rp4 + c4;
+                    const float4 po = a.p[vi], qo = a.q[vi];
+                    // eight independent neighbour gathers in flight per lane; the tail of
+                    // a row is predicated (a missing entry reads the own row times zero)
+                    for (int e = e0; e < e1; e += 8) {
+                        int cc[8];
+                        float4 mm[8], zz[8];
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            cc[u] = a.col[e + u];
-                            mm[u] = a.mA[e + u];
+                        for (int u = 0; u < 8; ++u) {
+                            const bool ok = e + u < e1;
+                            cc[u] = ok ? a.col[e + u] : row;
+                            mm[u] = ok ? a.mA[e + u] : make_float4(0.f, 0.f, 0.f, 0.f);
                         }
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) zz[u] = a.z[(size_t)cc[u] * Rp4 + c4];
+                        for (int u = 0; u < 8; ++u) zz[u] = a.z[(size_t)cc[u] * Rp4 + c4];
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) acc_entry(mm[u], zz[u]);
+                        for (int u = 0; u < 8; ++u) acc_entry(mm[u], zz[u]);
                     }
-                    for (; e < e1; ++e) acc_entry(a.mA[e], a.z[(size_t)a.col[e] * Rp4 + c4]);
-                    const size_t vi = (size_t)row * Rp4 + c4;
-                    const float4 zo = a.z[vi], po = a.p[vi], qo = a.q[vi];
+                    const float4 zo = a.z[vi];
                     const float zov[4] = {zo.x, zo.y, zo.z, zo.w}, pov[4] = {po.x, po.y, po.z, po.w},
                                 qov[4] = {qo.x, qo.y, qo.z, qo.w};
                     float pn[4], qn[4];
@@ -543,7 +708,7 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                 for (int j = 0; j < 2; ++j)
 #pragma unroll
                     for (int k = 0; k < kNV; ++k) rb[j][k] = KF{0.0f, 0.0f};
-                for (int g = g0; g < ngroups; g += gstride) {
+                for (int g = g0; g < gend; g += gstride) {
                     const int row = g * G + slot;
                     if (row >= a.n) continue;
                     const size_t vi = (size_t)row * Rp4 + c4;
@@ -595,24 +760,36 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
             for (int j = 0; j < 2; ++j)
 #pragma unroll
                 for (int k = 0; k < kNV; ++k) ru[j][k] = KF{0.0f, 0.0f};
-            for (int g = g0; g < ngroups; g += gstride) {
+            for (int g = g0; g < gend; g += gstride) {
                 const int row = g * G + slot;
                 if (row >= a.n) continue;
                 DF ar[2], jx[2], jy[2], jz[2];
 #pragma unroll
                 for (int c = 0; c < 2; ++c) ar[c] = jx[c] = jy[c] = jz[c] = DF{0.0f, 0.0f};
                 const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
-                for (int e = e0; e < e1; ++e) {
-                    const int cidx = a.col[e];
-                    const float4 hi = a.mA[e], lo = a.mL[e];
-                    const float4 dd = a.dv[dsel][(size_t)cidx * Rp4 + c4];
-                    const float dc[2] = {dd.x - dd.w, dd.y + dd.z};  // d0 + i d1
+                for (int e = e0; e < e1; e += 4) {   // four gathers in flight, predicated tail
+                    int cc[4];
+                    float4 hi[4], lo[4], dd[4];
+                    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        df_fma(ar[c], hi.x, lo.x, dc[c], 0.0f);
-                        df_fma(jx[c], hi.y, lo.y, dc[c], 0.0f);
-                        df_fma(jy[c], hi.z, lo.z, dc[c], 0.0f);
-                        df_fma(jz[c], hi.w, lo.w, dc[c], 0.0f);
+                    for (int u = 0; u < 4; ++u) {
+                        const bool ok = e + u < e1;
+                        cc[u] = ok ? a.col[e + u] : row;
+                        hi[u] = ok ? a.mA[e + u] : z4;
+                        lo[u] = ok ? a.mL[e + u] : z4;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) dd[u] = a.dv[dsel][(size_t)cc[u] * Rp4 + c4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float dc[2] = {dd[u].x - dd[u].w, dd[u].y + dd[u].z};  // d0 + i d1
+#pragma unroll
+                        for (int c = 0; c < 2; ++c) {
+                            df_fma(ar[c], hi[u].x, lo[u].x, dc[c], 0.0f);
+                            df_fma(jx[c], hi[u].y, lo[u].y, dc[c], 0.0f);
+                            df_fma(jy[c], hi[u].z, lo[u].z, dc[c], 0.0f);
+                            df_fma(jz[c], hi[u].w, lo[u].w, dc[c], 0.0f);
+                        }
                     }
                 }
                 const size_t vi = (size_t)row * Rp4 + c4;
@@ -630,12 +807,17 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
                 const DF adi = df_add(df_norm(ar[1]), df_scale(jg[0], cn[0]));
                 const DF nr = df_add(DF{rh.x, rl.x}, df_neg(adr));
                 const DF ni = df_add(DF{rh.y, rl.y}, df_neg(adi));
-                const DF u_re = df_add(DF{uh.x, ul.x}, DF{dco[0], 0.0f});
-                const DF u_im = df_add(DF{uh.y, ul.y}, DF{dco[1], 0.0f});
+                // the history slot holds this step's total correction; in the first sweep
+                // it is the guess offset e, which enters u here
+                const float2 hc = Hc[vi];
+                const float2 eo = (sweep == 0) ? hc : make_float2(0.f, 0.f);
+                const DF u_re = df_add(df_add(DF{uh.x, ul.x}, DF{eo.x, 0.0f}), DF{dco[0], 0.0f});
+                const DF u_im = df_add(df_add(DF{uh.y, ul.y}, DF{eo.y, 0.0f}), DF{dco[1], 0.0f});
                 a.rh[vi] = make_float2(nr.h, ni.h);
                 a.rl[vi] = make_float2(nr.l, ni.l);
                 a.uh[vi] = make_float2(u_re.h, u_im.h);
                 a.ul[vi] = make_float2(u_re.l, u_im.l);
+                Hc[vi] = make_float2(hc.x + dco[0], hc.y + dco[1]);
                 const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
                 const float2 z0 = make_float2(dinv.x * nr.h, dinv.y * nr.h);
                 const float2 z1 = make_float2(dinv.x * ni.h, dinv.y * ni.h);
@@ -692,7 +874,7 @@ __global__ void __launch_bounds__(kThreadsB) k_batched(MixArgs a) {
     for (int j = 0; j < 2; ++j)
 #pragma unroll
         for (int k = 0; k <= kMaxCompartments; ++k) acc[j][k] = 0.0;
-    for (int g = g0; g < ngroups; g += gstride) {
+    for (int g = g0; g < gend; g += gstride) {
         const int row = g * G + slot;
         if (row >= a.n) continue;
         const size_t vi = (size_t)row * Rp4 + c4;
@@ -833,8 +1015,8 @@ static void map_status_mixed(int st) {
 
 // Launch one batch (R <= 512 signals) with the given geometry; n_steps may be
 // truncated for tuning.  Returns the device time of the stepper kernel (ms).
-static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int n_steps, double rtol,
-                          int maxit, const double* d_u0) {
+static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int blocked, int n_steps,
+                          double rtol, int maxit, const double* d_u0) {
     Mesh& m = ctx->mesh;
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
@@ -858,7 +1040,8 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     W.fin.alloc((size_t)Rp * kNV);
     const size_t nv = (size_t)m.n_dofs * Rp;
     for (auto* v : {&W.d0, &W.d1, &W.ri, &W.z, &W.p, &W.q}) v->alloc(nv);        // per slot
-    for (auto* v : {&W.uh, &W.ul, &W.rh, &W.rl}) v->alloc(nv / 2);               // per signal
+    for (auto* v : {&W.uh, &W.ul, &W.rh, &W.rl, &W.h0, &W.h1, &W.h2}) v->alloc(nv / 2);   // per signal
+    for (auto* v : {&W.h0, &W.h1, &W.h2}) v->zero(s);
     W.sig.alloc((size_t)Rp * (1 + kMaxCompartments));
     W.bar.alloc(2);
     W.status.alloc(1);
@@ -892,6 +1075,10 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     a.z = reinterpret_cast<float4*>(W.z.p);
     a.p = reinterpret_cast<float4*>(W.p.p);
     a.q = reinterpret_cast<float4*>(W.q.p);
+    a.hist[0] = W.h0.p;
+    a.hist[1] = W.h1.p;
+    a.hist[2] = W.h2.p;
+    a.extrap = ctx->opt_mixed_extrapolate;
     a.partials = W.partials;
     a.fin = W.fin;
     a.sigpart = W.sigpart;
@@ -912,14 +1099,15 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     a.rtol = (float)rtol;
     a.eps_first = (float)ctx->opt_mixed_eps_first;
     a.eps_next = (float)ctx->opt_mixed_eps_next;
-    a.two_stage = ((size_t)nb * Rp * kNV > 16384) ? 1 : 0;
+    a.two_stage = ((size_t)nb * Rp * kNV > 12288) ? 1 : 0;
+    a.blocked = blocked;
     a.iters = W.iters;
     a.sweeps = W.sweeps;
     a.sig = W.sig;
     a.diag = W.diag;
     {
         const void* need_ptrs[] = {a.row_ptr, a.col, a.mA, a.mL, a.mS, a.dg, a.w, a.rcomp, a.uh, a.ul, a.rh, a.rl,
-                                   a.dv[0], a.dv[1], a.ri, a.z, a.p, a.q, a.partials, a.fin, a.sigpart, a.bar,
+                                   a.dv[0], a.dv[1], a.ri, a.z, a.p, a.q, a.hist[0], a.hist[1], a.hist[2], a.partials, a.fin, a.sigpart, a.bar,
                                    a.status, a.fnew, a.fold, a.qv, a.gv, a.seqv, a.iters, a.sweeps, a.sig, a.diag};
         for (const void* ptr : need_ptrs)
             BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "mixed stepper: a device buffer is not allocated");
@@ -950,28 +1138,35 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     return ms;
 }
 
-// Measuring autotuner: for this (n, R) try every valid lanes-per-row with 1 and
-// the maximum co-resident blocks per SM on a 3-step run, keep the fastest.
-static std::pair<int, int> autotune_mixed(bt_ctx* ctx, SolverMixed& W, int R, double rtol, int maxit,
-                                          const double* d_u0) {
-    if (ctx->opt_mixed_lpr > 0)
-        return {ctx->opt_mixed_lpr, ctx->opt_mixed_blocks_per_sm > 0 ? ctx->opt_mixed_blocks_per_sm : 2};
+// Measuring autotuner: for this (n, R) try every valid lanes-per-row, 1 and 2
+// blocks per SM, and interleaved or blocked row ownership on a 3-step run; keep
+// the fastest.  Options fix any of the three.
+static SolverMixed::Geo autotune_mixed(bt_ctx* ctx, SolverMixed& W, int R, double rtol, int maxit,
+                                       const double* d_u0) {
     const auto key = std::make_pair(ctx->mesh.n_dofs, R);
     auto it = W.tuned.find(key);
     if (it != W.tuned.end()) return it->second;
-    std::pair<int, int> best{-1, 1};
-    float best_ms = 1e30f;
-    const int steps = std::min(3, ctx->sched.n_steps);
-    for (int lpr : lpr_candidates(R)) {
-        for (int bps : {1, 2, 4}) {
-            const float ms = launch_batch(ctx, W, R, lpr, bps, steps, rtol, maxit, d_u0);
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = {lpr, bps};
-            }
-        }
+    std::vector<int> lprs = lpr_candidates(R), bpss = {1, 2}, blks = {0, 1};
+    if (ctx->opt_mixed_lpr > 0) lprs = {ctx->opt_mixed_lpr};
+    if (ctx->opt_mixed_blocks_per_sm > 0) bpss = {ctx->opt_mixed_blocks_per_sm};
+    if (ctx->opt_mixed_blocked >= 0) blks = {ctx->opt_mixed_blocked};
+    SolverMixed::Geo best{-1, 1, 0};
+    if (lprs.size() * bpss.size() * blks.size() == 1) {
+        best = {lprs[0], bpss[0], blks[0]};
+    } else {
+        float best_ms = 1e30f;
+        const int steps = std::min(3, ctx->sched.n_steps);
+        for (int lpr : lprs)
+            for (int bps : bpss)
+                for (int blk : blks) {
+                    const float ms = launch_batch(ctx, W, R, lpr, bps, blk, steps, rtol, maxit, d_u0);
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = {lpr, bps, blk};
+                    }
+                }
     }
-    BT_REQUIRE(best.first > 0, BT_ERR_INVALID, "mixed stepper: no valid geometry for this batch size");
+    BT_REQUIRE(best.lpr > 0, BT_ERR_INVALID, "mixed stepper: no valid geometry for this batch size");
     W.tuned[key] = best;
     return best;
 }
@@ -1039,7 +1234,7 @@ void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir,
         W.gv.upload(hg.data(), (size_t)Rmax * 3, s);
         W.seqv.upload(hs.data(), Rmax, s);
         const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, d_u0);
-        const float ms = launch_batch(ctx, W, R, geo.first, geo.second, S.n_steps, rtol, maxit, d_u0);
+        const float ms = launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, S.n_steps, rtol, maxit, d_u0);
         stepper_ms += ms;
         const int Rp = W.Rp;
         std::vector<double> hsig((size_t)Rp * (1 + kMaxCompartments));
@@ -1095,6 +1290,10 @@ void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u) {
         u[2 * i] = src[i].x;
         u[2 * i + 1] = src[i].y;
     }
+}
+
+void reset_tuning_mixed(bt_ctx* ctx) {
+    if (ctx->smx) ctx->smx->tuned.clear();
 }
 
 void free_solver_mixed(bt_ctx* ctx) {

@@ -172,6 +172,8 @@ struct bt_ctx {
     int opt_mixed_max_sweeps = 8;
     double opt_mixed_eps_first = 1e-4;
     double opt_mixed_eps_next = 3e-3;
+    int opt_mixed_extrapolate = 2;
+    int opt_mixed_blocked = -1;
     int opt_fp64_extrapolate = 1;
 };
 
@@ -192,6 +194,7 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
                   bt_stats* st);
 void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u);
+void reset_tuning_mixed(bt_ctx* ctx);
 void free_solvers(bt_ctx* ctx);
 double device_sum(const double* d, int64_t n, cudaStream_t s);
 double device_dot(const double* a, const double* b, int64_t n, cudaStream_t s);

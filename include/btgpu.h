@@ -171,6 +171,9 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *   "mixed.max_sweeps"      refinement sweeps per step (default 8)
  *   "mixed.eps_first"       inner FP32 tolerance of the first sweep (1e-4)
  *   "mixed.eps_next"        inner FP32 tolerance of later sweeps (3e-3)
+ *   "mixed.blocked_rows"    rows of a block: 1 contiguous range, 0 interleaved, -1 tuned (default)
+ *   "mixed.extrapolate"     initial guess of each step: 2 = 3u_n - 3u_{n-1} + u_{n-2} (default),
+ *                           1 = 2u_n - u_{n-1}, 0 = u_n
  *   "fp64.extrapolate"      1: initial guess 2 u_n - u_{n-1} (default), 0: u_n */
 int bt_set_option(bt_ctx* ctx, const char* key, double value);
 

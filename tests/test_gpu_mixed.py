@@ -39,7 +39,7 @@ def test_mixed_matches_golden(pkg, lib, golden):
         q = [s["q"] for s in sig]
         g = [s["gdir"] for s in sig]
         pidx = [s["profile"] for s in sig]
-        out = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-8, max_iterations=2000,
+        out = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-9, max_iterations=2000,
                         compartments=True)
         for k, s in enumerate(sig):
             got = out["signal"][k] / out["S0"]
@@ -56,7 +56,7 @@ def test_mixed_batches_match_fp64(pkg, lib, nsig):
     ctx = ctx_for(pkg, w)
     idx = np.linspace(0, len(w["signals"]) - 1, nsig).astype(int)
     q, g, pidx = signals_of(pkg, w, idx)
-    mixed = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-8, compartments=True)
+    mixed = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-9, compartments=True)
     fp64 = ctx.solve(q, g, pidx, precision=pkg.PRECISION_FP64, rtol=1e-12, compartments=True)
     rel = np.abs(mixed["signal"] - fp64["signal"]) / np.abs(fp64["signal"])
     assert rel.max() <= MIX_RTOL, rel.max()
@@ -68,9 +68,9 @@ def test_mixed_deterministic_and_solution(pkg, lib):
     w = pkg.meshgen.workload("cfg4", n=10)
     ctx = ctx_for(pkg, w)
     q, g, pidx = signals_of(pkg, w, range(0, 120, 9))
-    a = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-8)
+    a = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-9)
     ua = ctx.solution(3)
-    b = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-8)
+    b = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-9)
     ub = ctx.solution(3)
     assert np.array_equal(a["signal"], b["signal"]) and np.array_equal(ua, ub)
     ref = ctx.solve(q, g, pidx, precision=pkg.PRECISION_FP64, rtol=1e-12)
@@ -83,6 +83,6 @@ def test_mixed_deterministic_and_solution(pkg, lib):
 def test_mixed_b0_is_one(pkg, lib):
     w = pkg.meshgen.workload("cfg2", n=8)
     ctx = ctx_for(pkg, w)
-    out = ctx.solve([0.0, 0.0, 0.0], [[1, 0, 0]] * 3, precision=pkg.PRECISION_MIXED, rtol=1e-8)
+    out = ctx.solve([0.0, 0.0, 0.0], [[1, 0, 0]] * 3, precision=pkg.PRECISION_MIXED, rtol=1e-9)
     assert np.all(np.abs(out["signal"] / out["S0"] - 1.0) < 1e-9)
     ctx.close()
