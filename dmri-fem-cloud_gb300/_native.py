@@ -32,7 +32,7 @@ EXPORTS = [
     "bt_mesh_upload", "bt_mesh_info", "bt_set_coefficients", "bt_set_cell_diffusion",
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
-    "bt_signal_noalloc", "bt_adjoint",
+    "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi",
 ]
 
 
@@ -103,6 +103,8 @@ def load(path=None):
         "bt_signal_noalloc": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
         "bt_adjoint": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_double, C.c_int32, C.c_int32,
                                  _D, _D, _D, _D, C.POINTER(Stats)]),
+        "bt_solve_multi": (C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _D, _I32, C.c_double, C.c_int32,
+                                     _D, _D, C.POINTER(Stats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -272,3 +274,30 @@ class Context:
         it = np.zeros(n_signals * n_steps, np.int32)
         self._check(self.lib.bt_get_iterations(self.h, _ip(it), it.size))
         return it.reshape(n_signals, n_steps)
+
+
+def solve_multi(contexts, q, gdir, sequence=None, rtol=1e-9, max_iterations=5000):
+    """Several meshes in one persistent mixed-precision launch.
+
+    ``contexts[m]`` holds mesh m (uploaded, assembled, with a schedule);
+    ``q[m]``, ``gdir[m]`` (and ``sequence[m]``) are that mesh's signals.
+    Returns {"signal": [array per mesh], "S0": array, "stats": dict}."""
+    nm = len(contexts)
+    qs = [np.atleast_1d(np.asarray(x, np.float64)) for x in q]
+    if len(qs) != nm or len(gdir) != nm:
+        raise ValueError("one q list and one gdir list per context")
+    nsig = np.ascontiguousarray([len(x) for x in qs], np.int32)
+    qa = np.ascontiguousarray(np.concatenate(qs))
+    ga = np.ascontiguousarray(np.concatenate([np.asarray(g, np.float64).reshape(len(x), 3)
+                                              for g, x in zip(gdir, qs)]))
+    sa = None if sequence is None else np.ascontiguousarray(
+        np.concatenate([np.asarray(s_, np.int32).reshape(len(x)) for s_, x in zip(sequence, qs)]))
+    handles = (_P * nm)(*[c.h for c in contexts])
+    sig = np.zeros(len(qa))
+    S0 = np.zeros(nm)
+    st = Stats()
+    lib = contexts[0].lib
+    contexts[0]._check(lib.bt_solve_multi(handles, nm, _ip(nsig), _dp(qa), _dp(ga), _ip(sa), float(rtol),
+                                          int(max_iterations), _dp(sig), _dp(S0), C.byref(st)))
+    cuts = np.cumsum(nsig)[:-1]
+    return {"signal": np.split(sig, cuts), "S0": S0, "stats": st.as_dict()}

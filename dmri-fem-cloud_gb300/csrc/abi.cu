@@ -36,6 +36,11 @@ void use_device(bt_ctx* ctx) { BT_CUDA(cudaSetDevice(ctx->device)); }
 
 }  // namespace
 
+std::mutex& bt::persistent_kernel_mutex() {
+    static std::mutex mu;
+    return mu;
+}
+
 extern "C" {
 
 int bt_version(void) { return 100; }
@@ -259,6 +264,52 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
             } else {
                 *S0_out = ctx->mesh.volume;
             }
+        }
+    });
+}
+
+int bt_solve_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_signals, const double* q,
+                   const double* gdir, const int32_t* sequence, double rtol, int32_t max_iterations,
+                   double* signal_out, double* S0_out, bt_stats* stats) {
+    if (!contexts || n_meshes < 1 || !contexts[0]) return BT_ERR_INVALID;
+    bt_ctx* c0 = contexts[0];
+    return guarded(c0, [&] {
+        BT_REQUIRE(n_meshes <= 64 && n_signals && q && gdir && signal_out, BT_ERR_INVALID,
+                   "bt_solve_multi: bad arguments (at most 64 meshes)");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_solve_multi: rtol must be > 0 and max_iterations >= 1");
+        int64_t total = 0;
+        for (int32_t m = 0; m < n_meshes; ++m) {
+            bt_ctx* c = contexts[m];
+            BT_REQUIRE(c != nullptr, BT_ERR_INVALID, "bt_solve_multi: null context");
+            for (int32_t j = 0; j < m; ++j)
+                BT_REQUIRE(contexts[j] != c, BT_ERR_INVALID, "bt_solve_multi: a context is listed twice");
+            BT_REQUIRE(c->device == c0->device, BT_ERR_INVALID, "bt_solve_multi: contexts on different devices");
+            BT_REQUIRE(c->mesh.built && c->mat.done && c->sched.set, BT_ERR_STATE,
+                       "bt_solve_multi: every mesh needs bt_assemble and bt_set_schedule");
+            BT_REQUIRE(n_signals[m] >= 1 && n_signals[m] <= 256, BT_ERR_INVALID,
+                       "bt_solve_multi: 1..256 signals per mesh");
+            total += n_signals[m];
+        }
+        for (int64_t i = 0; i < total; ++i) {
+            BT_REQUIRE(std::isfinite(q[i]) && std::isfinite(gdir[3 * i]) && std::isfinite(gdir[3 * i + 1]) &&
+                           std::isfinite(gdir[3 * i + 2]),
+                       BT_ERR_INVALID, "bt_solve_multi: q and gradient directions must be finite");
+            if (sequence) {
+                int64_t acc = 0;
+                int32_t m = 0;
+                while (acc + n_signals[m] <= i) acc += n_signals[m++];
+                BT_REQUIRE(sequence[i] >= 0 && sequence[i] < contexts[m]->sched.n_seq, BT_ERR_INVALID,
+                           "bt_solve_multi: sequence index out of range");
+            }
+        }
+        use_device(c0);
+        for (int32_t m = 0; m < n_meshes; ++m) contexts[m]->last_precision = -1;
+        bt::solve_mixed_multi(contexts, n_meshes, n_signals, q, gdir, sequence, rtol, max_iterations, signal_out,
+                              stats);
+        for (int32_t m = 0; m < n_meshes; ++m) {
+            contexts[m]->last_precision = BT_PRECISION_MIXED;
+            if (S0_out) S0_out[m] = contexts[m]->mesh.volume;
         }
     });
 }

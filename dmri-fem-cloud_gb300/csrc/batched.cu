@@ -52,6 +52,8 @@ constexpr int kThreadsB = kWarpsB * 32;
 constexpr int kMaxRhs = 512;
 constexpr int kNV = 4;  // values per RHS in one reduction
 
+struct MixArgs;
+
 struct SolverMixed {
     int64_t n = 0;
     int32_t Rp = 0;
@@ -82,6 +84,8 @@ struct SolverMixed {
         int lpr, per_sm, blocked;
     };
     std::map<std::pair<int64_t, int32_t>, Geo> tuned;  // (n, R) -> launch geometry
+    DevBuf<MixArgs> margs;   // several meshes in one launch (kept by the first mesh's context)
+    DevBuf<int> mfirst;
 };
 
 struct MixArgs {
@@ -232,7 +236,7 @@ __device__ __forceinline__ float2 dfa(float2 a, float2 b) {  // (hi, lo) + (hi, 
 
 template <int LPR>
 __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV], const MixArgs& a, int chunk,
-                                           int r0, unsigned nb, unsigned& gen, float2* smem) {
+                                           int r0, unsigned nb, unsigned bid, unsigned& gen, float2* smem) {
     constexpr int C = 2 * LPR;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     float2 d[2][kNV];
@@ -269,15 +273,15 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
         const int c = r / C, o = r % C;
         float2 s = make_float2(0.f, 0.f);
         for (int wb = 0; wb < kWarpsB; ++wb)
-            if ((int)((blockIdx.x * kWarpsB + wb) % nchunks) == c) s = dfa(s, smem[(wb * C + o) * kNV + k]);
-        a.partials[(size_t)blockIdx.x * a.Rp * kNV + t] = s;
+            if ((int)((bid * kWarpsB + wb) % nchunks) == c) s = dfa(s, smem[(wb * C + o) * kNV + k]);
+        a.partials[(size_t)bid * a.Rp * kNV + t] = s;
     }
     const int V = a.Rp * kNV;
     if (a.two_stage) {
         if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
         // stage 2: one warp per value; lane l adds blocks l, l+32, ... and the
         // warp combines the 32 lane sums in a fixed butterfly (lane 0's order)
-        const int gw = blockIdx.x * kWarpsB + wib;
+        const int gw = bid * kWarpsB + wib;
         for (int t = gw; t < V; t += nb * kWarpsB) {
             float2 s = make_float2(0.f, 0.f);
             for (unsigned b0 = lane; b0 < nb; b0 += 4u * 32u) {
@@ -310,6 +314,11 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
         // others, which read only the V sums
         __shared__ int s_last, s_ok;
         const unsigned target = gen + 1;
+        // every thread makes its own stores (this phase's vectors and the partials)
+        // visible device-wide before the block arrives: the arrival is one thread's
+        // release, and we do not rely on it covering the other warps' stores
+        __threadfence();
+        __syncthreads();
         if (threadIdx.x == 0) {
             // no status check before arriving (it would cost a round trip): a block
             // that left on an error never arrives, and the waiters below see the
@@ -341,6 +350,7 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
                 if (part == 0 && t < V) {
                     smem[t] = s;
                     __stcg(&a.fin[t], s);
+                    __threadfence();
                 }
             }
             __syncthreads();
@@ -378,16 +388,17 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
 }
 
 // ------------------------------------------------------------------ kernel ----
+// The stepper on one mesh, run by blocks bid = 0..nb-1 of a (sub-)grid whose
+// blocks are all co-resident.
 template <int LPR>
-__global__ void __maxnreg__(120) k_batched(MixArgs a) {
+__device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bid, const unsigned nb) {
     constexpr int G = 32 / LPR;  // rows per warp-unit
     constexpr int C = 2 * LPR;   // RHS per warp-unit
     __shared__ float2 smem[kWarpsB * 64 * kNV > kMaxRhs * kNV ? kWarpsB * 64 * kNV : kMaxRhs * kNV];
     __shared__ int s_flag;
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * kWarpsB + (threadIdx.x >> 5);
-    const int total_warps = gridDim.x * kWarpsB;
-    const unsigned nb = gridDim.x;
+    const int gw = bid * kWarpsB + (threadIdx.x >> 5);
+    const int total_warps = nb * kWarpsB;
     const int nchunks = a.Rp / C;
     const int chunk = gw % nchunks;
     const int slot = lane / LPR;
@@ -400,8 +411,8 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
     // groups, so the neighbour rows its warps gather overlap and are reused in L1.
     int g0, gend, gstride;
     if (a.blocked) {
-        g0 = (int)(((long long)ngroups * blockIdx.x) / nb) + (threadIdx.x >> 5) / nchunks;
-        gend = (int)(((long long)ngroups * (blockIdx.x + 1)) / nb);
+        g0 = (int)(((long long)ngroups * bid) / nb) + (threadIdx.x >> 5) / nchunks;
+        gend = (int)(((long long)ngroups * (bid + 1)) / nb);
         gstride = kWarpsB / nchunks;
     } else {
         g0 = gw / nchunks;
@@ -429,7 +440,7 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
 #define BT_REDUCE(V, OUT)                                                     \
     do {                                                                      \
         b.partials = (flip++ & 1u) ? part1 : part0;                           \
-        if (!reduce_rhs<LPR>(V, OUT, b, chunk, r0, nb, gen, smem)) return;    \
+        if (!reduce_rhs<LPR>(V, OUT, b, chunk, r0, nb, bid, gen, smem)) return; \
     } while (0)
 
     int dsel = 0;
@@ -500,8 +511,10 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
         //      history slot of this step and added to u by the first phase U.
         const float c1 = (a.extrap == 0 || step == 0) ? 0.f : ((a.extrap == 1 || step == 1) ? 1.f : 2.f);
         const float c2 = (a.extrap == 2 && step >= 2) ? -1.f : 0.f;
-        const float2* __restrict__ H1 = a.hist[(step + 2) % 3];
-        const float2* __restrict__ H2 = a.hist[(step + 1) % 3];
+        // the history is written inside this kernel: read it coherently (L2), never
+        // through the read-only path
+        const float2* H1 = a.hist[(step + 2) % 3];
+        const float2* H2 = a.hist[(step + 1) % 3];
         float2* const Hc = a.hist[step % 3];
         KF red[2][kNV];
 #pragma unroll
@@ -533,8 +546,8 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const size_t ni = (size_t)cc[u] * Rp4 + c4;
-                        h1[u] = H1[ni];
-                        h2[u] = H2[ni];
+                        h1[u] = __ldcg(&H1[ni]);
+                        h2[u] = __ldcg(&H2[ni]);
                     }
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
@@ -549,7 +562,7 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
                         }
                     }
                 }
-                ev = guess_offset(H1[vi], H2[vi], c1, c2);
+                ev = guess_offset(__ldcg(&H1[vi]), __ldcg(&H2[vi]), c1, c2);
             }
             DF jg[2];
 #pragma unroll
@@ -620,7 +633,7 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
                     if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
 #pragma unroll
                     for (int j = 0; j < 2; ++j)
-                        if (blockIdx.x == 0 && act[j]) {
+                        if (bid == 0 && act[j]) {
                             a.diag[0] = 1.0f; a.diag[1] = (float)step; a.diag[2] = (float)sweep; a.diag[3] = (float)it;
                             a.diag[4] = rr2[j] / fmaxf(eps * eps * rrs[j], 1e-38f);
                             a.diag[5] = (float)(r0 / 2);
@@ -853,7 +866,7 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
             if (!s_flag) break;
             if (sweep >= a.max_sweeps) {
                 if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
-                if (blockIdx.x == 0 && r0 < a.R && rr2[0] + rr2[1] > tolb2[0]) {
+                if (bid == 0 && r0 < a.R && rr2[0] + rr2[1] > tolb2[0]) {
                     a.diag[0] = 2.0f; a.diag[1] = (float)step; a.diag[2] = (float)sweep; a.diag[3] = (float)it_total;
                     a.diag[4] = (rr2[0] + rr2[1]) / fmaxf(tolb2[0], 1e-38f); a.diag[5] = (float)(r0 / 2);
                 }
@@ -861,7 +874,7 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
                 break;
             }
         }
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (bid == 0 && threadIdx.x == 0) {
             a.iters[step] = it_total;
             a.sweeps[step] = sweep;
         }
@@ -905,7 +918,7 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
     }
     if (!grid_barrier(a.bar, nb, a.status, gen)) return;
     // grid thread t finishes (RHS r, value k): sum over warps of r's chunk in warp order
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gt = bid * blockDim.x + threadIdx.x;
     for (int t = gt; t < a.Rp * (1 + kMaxCompartments); t += nb * blockDim.x) {
         const int r = t / (1 + kMaxCompartments), k = t % (1 + kMaxCompartments);
         const int c = r / C, o = r % C;
@@ -914,6 +927,30 @@ __global__ void __maxnreg__(120) k_batched(MixArgs a) {
             s += __ldcg(&wp[((size_t)wv * C + o) * (1 + kMaxCompartments) + k]);
         a.sig[t] = s;
     }
+}
+
+template <int LPR>
+__global__ void __maxnreg__(120) k_batched(MixArgs a) {
+    batched_body<LPR>(a, blockIdx.x, gridDim.x);
+}
+
+// Several meshes in one cooperative launch: blocks first[m] .. first[m+1]-1 form
+// the sub-grid of mesh m, which runs its own stepper with its own barrier
+// counters and reductions; meshes never wait for one another.
+template <int LPR>
+__global__ void __maxnreg__(120) k_batched_multi(const MixArgs* __restrict__ args, const int* __restrict__ first,
+                                                 int n_meshes) {
+    __shared__ MixArgs s_a;
+    __shared__ int s_m;
+    if (threadIdx.x == 0) {
+        int m = 0;
+        while (m + 1 < n_meshes && (int)blockIdx.x >= first[m + 1]) ++m;
+        s_m = m;
+        s_a = args[m];
+    }
+    __syncthreads();
+    const int m = s_m;
+    batched_body<LPR>(s_a, blockIdx.x - first[m], first[m + 1] - first[m]);
 }
 
 // Pack the double-float matrix copies and the row data once per assembly/theta/dt.
@@ -963,6 +1000,18 @@ __global__ void k_rows_mixed(int64_t n, int32_t Rp, int32_t R, const int32_t* __
 namespace {
 
 using KFn = void (*)(MixArgs);
+using KFnMulti = void (*)(const MixArgs*, const int*, int);
+
+KFnMulti kernel_multi_for(int lpr) {
+    switch (lpr) {
+        case 1: return k_batched_multi<1>;
+        case 2: return k_batched_multi<2>;
+        case 4: return k_batched_multi<4>;
+        case 8: return k_batched_multi<8>;
+        case 16: return k_batched_multi<16>;
+        default: return k_batched_multi<32>;
+    }
+}
 
 KFn kernel_for(int lpr) {
     switch (lpr) {
@@ -1015,8 +1064,20 @@ static void map_status_mixed(int st) {
 
 // Launch one batch (R <= 512 signals) with the given geometry; n_steps may be
 // truncated for tuning.  Returns the device time of the stepper kernel (ms).
-static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int blocked, int n_steps,
-                          double rtol, int maxit, const double* d_u0) {
+// Warp-units of a batch on this mesh: row groups x RHS chunks.  A (sub-)grid of
+// more than units/8 blocks would leave blocks idle.
+static int blocks_needed(const bt_ctx* ctx, int R, int lpr) {
+    const int Rp = padded_rhs(R, lpr);
+    const int G = 32 / lpr;
+    const int64_t units = ((ctx->mesh.n_dofs + G - 1) / G) * (Rp / (2 * lpr));
+    return (int)std::max<int64_t>(1, (units + kWarpsB - 1) / kWarpsB);
+}
+
+// Buffers, initial state and kernel arguments of one batch of R slots on one
+// mesh, for a (sub-)grid of nb blocks; nothing is launched.  n_steps may be
+// truncated for tuning.
+static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb, int blocked, int n_steps,
+                             double rtol, int maxit, const double* d_u0) {
     Mesh& m = ctx->mesh;
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
@@ -1025,15 +1086,7 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     const int Rp = padded_rhs(R, lpr);
     BT_REQUIRE(Rp >= R && Rp <= kMaxRhs && (Rp / (2 * lpr)) <= kWarpsB && (kWarpsB % (Rp / (2 * lpr))) == 0,
                BT_ERR_INVALID, "mixed stepper: invalid RHS padding");
-    KFn fn = kernel_for(lpr);
-    int occ = 0;
-    BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
-    BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
-    const int per_sm = std::max(1, std::min(occ, per_sm_blocks));
-    const int G = 32 / lpr;
-    const int units = (int)(((m.n_dofs + G - 1) / G) * (Rp / (2 * lpr)));
-    const int need = std::max(1, (units + kWarpsB - 1) / kWarpsB);
-    const int nb = std::max(1, std::min(per_sm * ctx->num_sms, need));
+    BT_REQUIRE(nb >= 1, BT_ERR_INVALID, "mixed stepper: empty grid");
     // partials: two alternating float buffers [nb][Rp][kNV]
     W.partials.alloc((size_t)2 * nb * Rp * kNV);
     W.sigpart.alloc((size_t)nb * kWarpsB * 64 * (1 + kMaxCompartments));
@@ -1112,10 +1165,14 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
         for (const void* ptr : need_ptrs)
             BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "mixed stepper: a device buffer is not allocated");
     }
-    void* args[] = {&a};
-    BT_CUDA(cudaEventRecord(ctx->ev1, s));
-    BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(nb), dim3(kThreadsB), args, 0, s));
-    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    W.Rp = Rp;
+    W.nb = nb;
+    return a;
+}
+
+// Status of the last launch on this mesh (device status + failure report);
+// throws on failure.  The stream must be synchronised.
+static void check_batch(SolverMixed& W, int lpr, int nb, cudaStream_t s) {
     int hst = 0;
     float hdiag[8];
     BT_CUDA(cudaMemcpyAsync(&hst, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1131,10 +1188,28 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
         throw Error(BT_ERR_NOT_CONVERGED, msg);
     }
     map_status_mixed(hst);
+}
+
+// Launch one batch (R <= 512 slots) on one mesh with the given geometry.
+// Returns the device time of the stepper kernel (ms).
+static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int blocked, int n_steps,
+                          double rtol, int maxit, const double* d_u0) {
+    cudaStream_t s = ctx->stream;
+    KFn fn = kernel_for(lpr);
+    int occ = 0;
+    BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
+    BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
+    const int per_sm = std::max(1, std::min(occ, per_sm_blocks));
+    const int nb = std::max(1, std::min(per_sm * ctx->num_sms, blocks_needed(ctx, R, lpr)));
+    MixArgs a = prepare_batch(ctx, W, R, lpr, nb, blocked, n_steps, rtol, maxit, d_u0);
+    void* args[] = {&a};
+    std::lock_guard<std::mutex> lock(persistent_kernel_mutex());
+    BT_CUDA(cudaEventRecord(ctx->ev1, s));
+    BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(nb), dim3(kThreadsB), args, 0, s));
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    check_batch(W, lpr, nb, s);
     float ms = 0.0f;
     BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
-    W.Rp = Rp;
-    W.nb = nb;
     return ms;
 }
 
@@ -1171,8 +1246,8 @@ static SolverMixed::Geo autotune_mixed(bt_ctx* ctx, SolverMixed& W, int R, doubl
     return best;
 }
 
-void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
-                 const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st) {
+// Packed double-float matrices, row data and the schedule of this mesh.
+static SolverMixed& pack_mixed(bt_ctx* ctx, const double* u0, const double** d_u0) {
     Mesh& m = ctx->mesh;
     Assembled& A = ctx->mat;
     Schedule& S = ctx->sched;
@@ -1194,80 +1269,114 @@ void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir,
     W.fnew.upload(S.f_new.data(), S.f_new.size(), s);
     W.fold.upload(S.f_old.data(), S.f_old.size(), s);
     if (u0) W.u0.upload(u0, m.n_v, s);
-    const double* d_u0 = u0 ? W.u0.p : nullptr;
-    if (st) {
-        st->steps = S.n_steps;
-        st->max_iterations = 0;
-        st->total_iterations = 0;
-        st->max_rel_residual = rtol;
-        st->refinements = 0;
-        st->graph_launches = 0;
-        st->kernel_launches = 0;
-        st->stepper_ms = 0.0;
+    *d_u0 = u0 ? W.u0.p : nullptr;
+    return W;
+}
+
+// Slot parameters of NS signals (q, gdir, seq point at the first): slots 2r and
+// 2r+1 are Re and Im of signal r; all kMaxRhs slots are filled, the padding with
+// copies of the last signal (padding slots start from u = 0 and never iterate).
+static void upload_rhs(bt_ctx* ctx, SolverMixed& W, int NS, const double* q, const double* gdir,
+                       const int32_t* seq) {
+    cudaStream_t s = ctx->stream;
+    const int Rmax = kMaxRhs;
+    std::vector<double> hq(Rmax);
+    std::vector<float> hg(Rmax * 3);
+    std::vector<int32_t> hs(Rmax);
+    for (int r = 0; r < Rmax; ++r) {
+        const int src = std::min(r / 2, NS - 1);
+        hq[r] = q[src];
+        for (int k = 0; k < 3; ++k) hg[r * 3 + k] = (float)gdir[3 * src + k];
+        hs[r] = seq ? seq[src] : 0;
+        BT_REQUIRE(hs[r] >= 0 && hs[r] < ctx->sched.n_seq, BT_ERR_INVALID, "sequence index out of range");
     }
-    ctx->last_iters.assign((size_t)nsig * S.n_steps, 0);
-    // final states are kept for bt_get_solution only for modest batches (the
-    // copy is n_dofs x n_signals complex values through the host)
-    const bool keep = (int64_t)nsig * m.n_dofs <= (int64_t)8 * 1024 * 1024;
-    W.saved.assign(keep ? (size_t)nsig * m.n_dofs : 0, make_double2(0.0, 0.0));
+    W.qv.upload(hq.data(), Rmax, s);
+    W.gv.upload(hg.data(), (size_t)Rmax * 3, s);
+    W.seqv.upload(hs.data(), Rmax, s);
+}
+
+// Signals (sig[0..NS-1], comp_sig optional), per-step iteration counts and, when
+// `keep`, the final states of the last launch on this mesh; b0 is the index of
+// the batch's first signal among the mesh's signals.
+static void collect_batch(bt_ctx* ctx, SolverMixed& W, int b0, int NS, bool keep, double* sig, double* comp_sig,
+                          bt_stats* st) {
+    Mesh& m = ctx->mesh;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    std::vector<int32_t> hit(S.n_steps), hsw(S.n_steps);
+    const int Rp = W.Rp;
+    std::vector<double> hsig((size_t)Rp * (1 + kMaxCompartments));
+    W.sig.download(hsig.data(), hsig.size(), s);
+    W.iters.download(hit.data(), S.n_steps, s);
+    W.sweeps.download(hsw.data(), S.n_steps, s);
+    const int nsr = Rp / 2;   // signals per row in the per-signal arrays
+    std::vector<float2> huh(keep ? (size_t)m.n_dofs * nsr : 0), hul(keep ? (size_t)m.n_dofs * nsr : 0);
+    if (keep) {
+        W.uh.download(huh.data(), huh.size(), s);
+        W.ul.download(hul.data(), hul.size(), s);
+    }
+    BT_CUDA(cudaStreamSynchronize(s));
+    for (int r = 0; r < NS; ++r) {
+        const size_t so = (size_t)(2 * r) * (1 + kMaxCompartments);   // signal r lives in slot 2r
+        sig[r] = hsig[so];
+        if (comp_sig)
+            for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)r * m.n_comp + c] = hsig[so + 1 + c];
+        for (int64_t i = 0; keep && i < m.n_dofs; ++i) {
+            const float2 h = huh[(size_t)i * nsr + r], l = hul[(size_t)i * nsr + r];
+            W.saved[(size_t)(b0 + r) * m.n_dofs + i] = make_double2((double)h.x + l.x, (double)h.y + l.y);
+        }
+        for (int k = 0; k < S.n_steps; ++k) ctx->last_iters[(size_t)(b0 + r) * S.n_steps + k] = hit[k];
+    }
+    if (st) {
+        for (int k = 0; k < S.n_steps; ++k) {
+            st->max_iterations = std::max(st->max_iterations, hit[k]);
+            st->total_iterations += (int64_t)hit[k] * NS;
+            st->refinements += hsw[k];
+        }
+    }
+}
+
+static void reset_stats(bt_stats* st, int32_t steps, double rtol) {
+    if (!st) return;
+    st->steps = steps;
+    st->max_iterations = 0;
+    st->total_iterations = 0;
+    st->max_rel_residual = rtol;
+    st->refinements = 0;
+    st->graph_launches = 0;
+    st->kernel_launches = 0;
+    st->stepper_ms = 0.0;
+}
+
+// Final states are kept for bt_get_solution only for modest batches (the copy
+// is n_dofs x n_signals complex values through the host).
+static bool keep_states(bt_ctx* ctx, SolverMixed& W, int32_t nsig) {
+    const bool keep = (int64_t)nsig * ctx->mesh.n_dofs <= (int64_t)8 * 1024 * 1024;
+    W.saved.assign(keep ? (size_t)nsig * ctx->mesh.n_dofs : 0, make_double2(0.0, 0.0));
     W.saved_nsig = keep ? nsig : 0;
+    ctx->last_iters.assign((size_t)nsig * ctx->sched.n_steps, 0);
+    return keep;
+}
+
+void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
+                 const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st) {
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    const double* d_u0 = nullptr;
+    SolverMixed& W = pack_mixed(ctx, u0, &d_u0);
+    reset_stats(st, S.n_steps, rtol);
+    const bool keep = keep_states(ctx, W, nsig);
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
     float stepper_ms = 0.0f;
-    std::vector<int32_t> hit(S.n_steps), hsw(S.n_steps);
     for (int32_t b0 = 0; b0 < nsig; b0 += kMaxRhs / 2) {
         const int NS = std::min<int32_t>(kMaxRhs / 2, nsig - b0);   // signals in this launch
         const int R = 2 * NS;                                        // slots: Re and Im of each
-        // per-RHS parameters for all kMaxRhs slots, padded with copies of the last
-        // real RHS (padding slots start from u = 0 and never iterate)
-        const int Rmax = kMaxRhs;
-        std::vector<double> hq(Rmax);
-        std::vector<float> hg(Rmax * 3);
-        std::vector<int32_t> hs(Rmax);
-        for (int r = 0; r < Rmax; ++r) {
-            const int src = b0 + std::min(r / 2, NS - 1);
-            hq[r] = q[src];
-            for (int k = 0; k < 3; ++k) hg[r * 3 + k] = (float)gdir[3 * src + k];
-            hs[r] = seq ? seq[src] : 0;
-            BT_REQUIRE(hs[r] >= 0 && hs[r] < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
-        }
-        W.qv.upload(hq.data(), Rmax, s);
-        W.gv.upload(hg.data(), (size_t)Rmax * 3, s);
-        W.seqv.upload(hs.data(), Rmax, s);
+        upload_rhs(ctx, W, NS, q + b0, gdir + 3 * b0, seq ? seq + b0 : nullptr);
         const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, d_u0);
-        const float ms = launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, S.n_steps, rtol, maxit, d_u0);
-        stepper_ms += ms;
-        const int Rp = W.Rp;
-        std::vector<double> hsig((size_t)Rp * (1 + kMaxCompartments));
-        W.sig.download(hsig.data(), hsig.size(), s);
-        W.iters.download(hit.data(), S.n_steps, s);
-        W.sweeps.download(hsw.data(), S.n_steps, s);
-        // final solutions (hi + lo) for bt_get_solution
-        const int nsr = Rp / 2;   // signals per row in the per-signal arrays
-        std::vector<float2> huh(keep ? (size_t)m.n_dofs * nsr : 0), hul(keep ? (size_t)m.n_dofs * nsr : 0);
-        if (keep) {
-            W.uh.download(huh.data(), huh.size(), s);
-            W.ul.download(hul.data(), hul.size(), s);
-        }
-        BT_CUDA(cudaStreamSynchronize(s));
-        for (int r = 0; r < NS; ++r) {
-            const size_t so = (size_t)(2 * r) * (1 + kMaxCompartments);   // signal r lives in slot 2r
-            sig[b0 + r] = hsig[so];
-            if (comp_sig)
-                for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)(b0 + r) * m.n_comp + c] = hsig[so + 1 + c];
-            for (int64_t i = 0; keep && i < m.n_dofs; ++i) {
-                const float2 h = huh[(size_t)i * nsr + r], l = hul[(size_t)i * nsr + r];
-                W.saved[(size_t)(b0 + r) * m.n_dofs + i] = make_double2((double)h.x + l.x, (double)h.y + l.y);
-            }
-            for (int k = 0; k < S.n_steps; ++k) ctx->last_iters[(size_t)(b0 + r) * S.n_steps + k] = hit[k];
-        }
-        if (st) {
-            for (int k = 0; k < S.n_steps; ++k) {
-                st->max_iterations = std::max(st->max_iterations, hit[k]);
-                st->total_iterations += (int64_t)hit[k] * NS;
-                st->refinements += hsw[k];
-            }
-            st->kernel_launches += 3;
-        }
+        stepper_ms += launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, S.n_steps, rtol, maxit, d_u0);
+        collect_batch(ctx, W, b0, NS, keep, sig + b0, comp_sig ? comp_sig + (size_t)b0 * ctx->mesh.n_comp : nullptr,
+                      st);
+        if (st) st->kernel_launches += 3;
     }
     BT_CUDA(cudaEventRecord(ctx->ev2, s));
     BT_CUDA(cudaEventSynchronize(ctx->ev2));
@@ -1278,6 +1387,158 @@ void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir,
         st->stepper_ms = stepper_ms;
     }
     ctx->last_nsig = nsig;
+}
+
+// ---------------------------------------------------------------- several meshes
+// Blocks of one cooperative launch shared among meshes in proportion to the
+// estimated work of an iteration (matrix + vector bytes), weighted by n^(1/3)
+// for the iteration count growing with mesh refinement; every mesh gets at least
+// one block and none more than it can use.
+static std::vector<int> split_blocks(bt_ctx* const* ctxs, int nm, const std::vector<int>& R, int lpr, int total) {
+    BT_REQUIRE(nm <= total, BT_ERR_INVALID, "bt_solve_multi: more meshes than co-resident blocks");
+    std::vector<double> w(nm);
+    std::vector<int> need(nm), nb(nm);
+    double sw = 0.0;
+    for (int m = 0; m < nm; ++m) {
+        const Mesh& M = ctxs[m]->mesh;
+        const int Rp = padded_rhs(R[m], lpr);
+        w[m] = (20.0 * (double)M.nnz + 96.0 * (double)M.n_dofs * Rp) * std::cbrt((double)M.n_dofs);
+        need[m] = blocks_needed(ctxs[m], R[m], lpr);
+        sw += w[m];
+    }
+    int used = 0;
+    for (int m = 0; m < nm; ++m) {
+        nb[m] = std::max(1, std::min(need[m], (int)std::floor(total * w[m] / sw)));
+        used += nb[m];
+    }
+    while (used > total) {   // rounding up to one block each can overshoot
+        int j = (int)(std::max_element(nb.begin(), nb.end()) - nb.begin());
+        if (nb[j] <= 1) break;
+        --nb[j];
+        --used;
+    }
+    while (used < total) {   // leftovers to the mesh with the most work per block
+        int j = -1;
+        double best = 0.0;
+        for (int m = 0; m < nm; ++m)
+            if (nb[m] < need[m] && w[m] / nb[m] > best) {
+                best = w[m] / nb[m];
+                j = m;
+            }
+        if (j < 0) break;
+        ++nb[j];
+        ++used;
+    }
+    return nb;
+}
+
+// One launch of the multi-mesh kernel; returns its device time (ms).
+static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R, int lpr, int n_steps_cap,
+                          double rtol, int maxit, const std::vector<const double*>& d_u0) {
+    bt_ctx* c0 = ctxs[0];
+    cudaStream_t s = c0->stream;
+    KFnMulti fn = kernel_multi_for(lpr);
+    int occ = 0;
+    BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
+    BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
+    // One block per SM in total: with two blocks per SM, blocks of different meshes
+    // share an SM, and in that arrangement the stepper was observed to stagnate
+    // non-deterministically (one block per SM never did).
+    const int total = c0->num_sms;
+    const std::vector<int> nb = split_blocks(ctxs, nm, R, lpr, total);
+    std::vector<MixArgs> args(nm);
+    std::vector<int> first(nm + 1, 0);
+    for (int m = 0; m < nm; ++m) {
+        SolverMixed& W = *ctxs[m]->smx;
+        const int steps = std::min(n_steps_cap, ctxs[m]->sched.n_steps);
+        args[m] = prepare_batch(ctxs[m], W, R[m], lpr, nb[m], 0, steps, rtol, maxit, d_u0[m]);
+        first[m + 1] = first[m] + nb[m];
+    }
+    SolverMixed& W0 = *c0->smx;
+    W0.margs.upload(args.data(), nm, s);
+    W0.mfirst.upload(first.data(), nm + 1, s);
+    const MixArgs* pa = W0.margs.p;
+    const int* pf = W0.mfirst.p;
+    int nmi = nm;
+    void* kargs[] = {&pa, &pf, &nmi};
+    std::lock_guard<std::mutex> lock(persistent_kernel_mutex());
+    BT_CUDA(cudaEventRecord(c0->ev1, s));
+    BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(first[nm]), dim3(kThreadsB), kargs, 0, s));
+    BT_CUDA(cudaEventRecord(c0->ev2, s));
+    for (int m = 0; m < nm; ++m) check_batch(*ctxs[m]->smx, lpr, nb[m], s);
+    float ms = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&ms, c0->ev1, c0->ev2));
+    return ms;
+}
+
+void solve_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q, const double* gdir,
+                       const int32_t* seq, double rtol, int32_t maxit, double* sig, bt_stats* st) {
+    bt_ctx* c0 = ctxs[0];
+    cudaStream_t s = c0->stream;
+    // every mesh's work goes on the first context's stream for this call
+    std::vector<cudaStream_t> saved(nm);
+    for (int m = 0; m < nm; ++m) {
+        BT_CUDA(cudaStreamSynchronize(ctxs[m]->stream));
+        saved[m] = ctxs[m]->stream;
+        ctxs[m]->stream = s;
+    }
+    struct Restore {
+        bt_ctx* const* c;
+        std::vector<cudaStream_t>& v;
+        ~Restore() {
+            for (size_t m = 0; m < v.size(); ++m) c[m]->stream = v[m];
+        }
+    } restore{ctxs, saved};
+    std::vector<int> R(nm);
+    std::vector<const double*> d_u0(nm, nullptr);
+    std::vector<int64_t> off(nm + 1, 0);
+    std::vector<char> keep(nm);
+    int32_t steps = 0;
+    for (int m = 0; m < nm; ++m) {
+        off[m + 1] = off[m] + nsig[m];
+        R[m] = 2 * nsig[m];
+        SolverMixed& W = pack_mixed(ctxs[m], nullptr, &d_u0[m]);
+        upload_rhs(ctxs[m], W, nsig[m], q + off[m], gdir + 3 * off[m], seq ? seq + off[m] : nullptr);
+        keep[m] = keep_states(ctxs[m], W, nsig[m]);
+        steps = std::max(steps, ctxs[m]->sched.n_steps);
+    }
+    reset_stats(st, steps, rtol);
+    // a lanes-per-row every mesh's batch can use (small batches are padded to
+    // the chunk), chosen on 3-step runs
+    std::vector<int> cands;
+    for (int lpr = 1; lpr <= 32; lpr <<= 1) {
+        bool ok = true;
+        for (int m = 0; m < nm; ++m) ok = ok && padded_rhs(R[m], lpr) > 0;
+        if (ok) cands.push_back(lpr);
+    }
+    if (c0->opt_mixed_lpr > 0) cands = {c0->opt_mixed_lpr};
+    BT_REQUIRE(!cands.empty(), BT_ERR_INVALID, "bt_solve_multi: no lanes-per-row fits every mesh's batch");
+    int lpr = cands[0];
+    if (cands.size() > 1) {
+        float best = 1e30f;
+        for (int c : cands) {
+            const float ms = launch_multi(ctxs, nm, R, c, 3, rtol, maxit, d_u0);
+            if (ms < best) {
+                best = ms;
+                lpr = c;
+            }
+        }
+    }
+    BT_CUDA(cudaEventRecord(c0->ev0, s));
+    const float ms = launch_multi(ctxs, nm, R, lpr, 1 << 30, rtol, maxit, d_u0);
+    for (int m = 0; m < nm; ++m) {
+        collect_batch(ctxs[m], *ctxs[m]->smx, 0, nsig[m], keep[m] != 0, sig + off[m], nullptr, st);
+        ctxs[m]->last_nsig = nsig[m];
+    }
+    BT_CUDA(cudaEventRecord(c0->ev2, s));
+    BT_CUDA(cudaEventSynchronize(c0->ev2));
+    float total = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&total, c0->ev0, c0->ev2));
+    if (st) {
+        st->gpu_ms = total;
+        st->stepper_ms = ms;
+        st->kernel_launches = 2 * nm + 1;
+    }
 }
 
 void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u) {

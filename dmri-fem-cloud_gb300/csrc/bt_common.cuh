@@ -4,6 +4,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <mutex>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -194,7 +196,13 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
                   bt_stats* st);
 void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u);
+void solve_mixed_multi(bt_ctx* const* ctxs, int32_t n_meshes, const int32_t* nsig, const double* q,
+                       const double* gdir, const int32_t* seq, double rtol, int32_t maxit, double* sig,
+                       bt_stats* st);
 void reset_tuning_mixed(bt_ctx* ctx);
+// Held from the launch of a persistent (grid-barrier) kernel until its stream has
+// drained: two such grids of this library never share the GPU's SMs.
+std::mutex& persistent_kernel_mutex();
 void free_solvers(bt_ctx* ctx);
 double device_sum(const double* d, int64_t n, cudaStream_t s);
 double device_dot(const double* a, const double* b, int64_t n, cudaStream_t s);
@@ -256,6 +264,7 @@ constexpr unsigned kBarrierMaxSpins = 1u << 26;
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status,
                                              unsigned& gen) {
     __shared__ int s_ok;
+    __threadfence();   // each thread's own stores are device-visible before its block arrives
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;

@@ -78,7 +78,10 @@ def fibonacci_directions(n):
 def random_cylinders(rng, half, rmin, rmax, count=None, volume_fraction=None, max_tries=20000):
     """Non-overlapping z-cylinders inside the square [-half, half]^2 (rejection
     sampling on centre distance > r1 + r2), either ``count`` of them or until
-    their area fraction reaches ``volume_fraction``."""
+    their area fraction reaches ``volume_fraction``.  Radii are capped at
+    0.9 half so that a cylinder always fits (small test boxes)."""
+    rmax = min(rmax, 0.9 * half)
+    rmin = min(rmin, rmax)
     cs, rs = [], []
     area = 0.0
     tries = 0
@@ -149,15 +152,16 @@ def workload(name, seed=0, n=None):
     raise ValueError("unknown workload %r" % name)
 
 
-def uneven_meshes(count=16, seed=0, nmin=24, nmax=96):
-    """Meshes of the uneven batch: edge counts stepped evenly from nmin to nmax,
-    random non-overlapping z-cylinders (radii U[1.5,5]) up to an area fraction
-    drawn from U[0.1,0.4], kappa ~ U[1e-5,1e-4], D_in = 2e-3, D_out = 3e-3."""
+def uneven_meshes(count=16, seed=0, nmin=24, nmax=96, cube=0.5):
+    """Meshes of the uneven batch: edge counts stepped evenly from nmin to nmax
+    (cubes of edge ``cube`` um), random non-overlapping z-cylinders (radii
+    U[1.5,5]) up to an area fraction drawn from U[0.1,0.4], kappa ~
+    U[1e-5,1e-4], D_in = 2e-3, D_out = 3e-3."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         n = int(round(nmin + (nmax - nmin) * i / max(1, count - 1)))
-        half = 0.25 * n          # 0.5 um cubes
+        half = 0.5 * cube * n
         xyz, tets = kuhn_box(-half, half, n)
         vf = rng.uniform(0.1, 0.4)
         cs, rs = random_cylinders(rng, half, 1.5, 5.0, volume_fraction=vf)

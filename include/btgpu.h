@@ -150,6 +150,21 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
              double rtol, int32_t max_iterations, double* signal_out,
              double* compartment_out, double* S0_out, bt_stats* stats);
 
+/* Several meshes in one persistent launch (mixed precision): mesh m is the
+ * mesh, coefficients, assembly and schedule of contexts[m] and gets
+ * n_signals[m] (1..256) signals; q, gdir, sequence and signal_out list the
+ * signals mesh by mesh.  The launch's blocks are split among the meshes in
+ * proportion to their work; each mesh advances with its own grid barrier and
+ * reductions, so meshes of uneven size and iteration count never wait for one
+ * another.  u0 = 1 on every mesh; S0_out[n_meshes] (or NULL) receives the
+ * volumes.  All contexts must be on one device; the work runs on the first
+ * context's stream and errors are reported there.  At most 64 meshes.  The
+ * reference integrates one mesh per MPI job (GCloudDmriSolver.py); it has no
+ * batched counterpart. */
+int bt_solve_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_signals,
+                   const double* q, const double* gdir, const int32_t* sequence, double rtol,
+                   int32_t max_iterations, double* signal_out, double* S0_out, bt_stats* stats);
+
 /* Discrete adjoint of the FP64 solve of one signal: the signal and its
  * derivatives with respect to the per-region isotropic D (dS_dD[n_regions]),
  * 1/T2 (dS_dinvT2[n_regions]) and the permeability of each region pair
