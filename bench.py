@@ -18,6 +18,10 @@ measurement through the public C-ABI calls from host buffers (mesh upload and
 device graph build, coefficient upload, assembly, schedule, solve, signals back
 to the host).
 
+``batched`` is the batched form on the eight-cylinder 64^3 workload: 64 of its
+512 signals (Fibonacci directions x b-values, PGSE and cos-OGSE) in one
+mixed-precision launch against the FP64 path on two of the same signals.
+
 ``--impl reference`` times the CPU restatement of the reference's solve path
 (two-field real system, Jacobi-BiCGSTAB rtol 1e-9 as GCloudDmriSolver.py
 ships it) with one process per host core, on a bounded sample of time steps.
@@ -296,6 +300,8 @@ def gpu_run(args):
         plain["mixed_over_plain"] = value / plain["value"]
         plain["max_rel_err_mixed_vs_fp64"] = float(np.max(np.abs(norm - n64) / np.abs(n64)))
 
+    batched = batched_leg(args, pkg, stream, flush, peak, peak_src) if args.batched_signals > 0 else None
+
     # end to end through the public C-ABI from host buffers
     e2e_ms = []
     h2d = (w["xyz"].nbytes + w["tets"].astype(np.int32).nbytes + w["region"].astype(np.int32).nbytes
@@ -336,6 +342,7 @@ def gpu_run(args):
             "iterations_per_signal": st["total_iterations"] / n_sig,
             "roofline": roof,
             "plain_fp64": plain,
+            "batched": batched,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "signals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
@@ -349,6 +356,66 @@ def gpu_run(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return res
+
+
+def batched_leg(args, pkg, stream, flush, peak, peak_src):
+    """The batched form on the eight-cylinder 64^3 workload: the first
+    `batched_signals` of its 512 signals (directions x b-values, PGSE and
+    cos-OGSE) in one mixed-precision launch, against the FP64 path on two of the
+    same signals (one FP64 launch per signal).  L2 flushed before each timed
+    launch."""
+    import torch
+    w = pkg.meshgen.workload("cfg3")
+    prof = w["profiles"]
+    fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in prof])
+    int4 = [p.int4gb() for p in prof]
+    sig = w["signals"]
+    idx = np.linspace(0, len(sig) - 1, args.batched_signals).astype(int)
+    sel = [sig[i] for i in idx]
+    q = np.array([pkg.sequences.b_to_q(b, int4[pi]) for b, _, pi in sel])
+    g = np.array([gd for _, gd, _ in sel], np.float64)
+    g /= np.linalg.norm(g, axis=1, keepdims=True)
+    pidx = np.array([pi for _, _, pi in sel], np.int32)
+    ctx = pkg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    ctx.set_stream(stream.cuda_stream)
+    ctx.mesh_upload(w["xyz"], w["tets"], w["region"], w["n_regions"], None)
+    ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
+    ctx.assemble()
+    ctx.set_schedule(np.array(fns), np.array(fos), w["dt"])
+    info = ctx.info()
+
+    def timed(fn):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    ctx.solve(q, g, pidx, None, pkg.PRECISION_MIXED, 1e-9, args.maxit)          # warm-up (autotuner)
+    ms_mix, out = timed(lambda: ctx.solve(q, g, pidx, None, pkg.PRECISION_MIXED, 1e-9, args.maxit))
+    two = [0, len(q) - 1]
+    ms_64, o64 = timed(lambda: ctx.solve(q[two], g[two], pidx[two], None, pkg.PRECISION_FP64, 1e-12, args.maxit))
+    st = out["stats"]
+    n_sig = len(q)
+    iters = st["total_iterations"] / n_sig
+    byts = alg_bytes_mixed(info["n_dofs"], info["nnz"], n_sig, st["steps"], iters, st["refinements"])
+    ach = byts / (st["stepper_ms"] / 1e3) / 1e9
+    err = float(np.max(np.abs(out["signal"][two] - o64["signal"]) / np.abs(o64["signal"])))
+    v_mix = n_sig / (ms_mix / 1e3)
+    v_64 = len(two) / (ms_64 / 1e3)
+    ctx.close()
+    return {"workload": "cfg3: " + WORKLOADS["cfg3"], "signals": n_sig, "n_dofs": info["n_dofs"], "nnz": info["nnz"],
+            "value": v_mix, "unit": "signals/s", "ms": ms_mix,
+            "plain_fp64_value": v_64, "plain_fp64_signals_timed": len(two),
+            "mixed_over_plain": v_mix / v_64, "max_rel_err_mixed_vs_fp64": err,
+            "iterations_per_signal": iters, "refinements": st["refinements"],
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "bytes_per_launch": byts, "launch_ms": st["stepper_ms"],
+                         "peak_source": peak_src + " hbm_gbs (copy)",
+                         "note": "algorithmic bytes (bench.alg_bytes_mixed); working set larger than L2"}}
 
 
 def reference_run(args):
@@ -387,6 +454,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample-steps", type=int, default=8)
     ap.add_argument("--cpu-sample-steps-ref", type=int, default=6)
+    ap.add_argument("--batched-signals", type=int, default=64,
+                    help="signals of the eight-cylinder 64^3 batched leg (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     args.warmup_e2e = 0

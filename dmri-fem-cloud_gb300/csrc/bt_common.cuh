@@ -172,8 +172,8 @@ struct bt_ctx {
     int opt_mixed_lpr = -1;
     int opt_mixed_blocks_per_sm = -1;
     int opt_mixed_max_sweeps = 8;
-    double opt_mixed_eps_first = 1e-4;
-    double opt_mixed_eps_next = 3e-3;
+    double opt_mixed_eps_first = 3e-6;
+    double opt_mixed_eps_next = 1e-2;
     int opt_mixed_extrapolate = 2;
     int opt_mixed_blocked = -1;
     int opt_fp64_extrapolate = 1;

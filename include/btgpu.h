@@ -184,8 +184,8 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *   "mixed.lanes_per_row"   1,2,4,...,32 (0: autotune, the default)
  *   "mixed.blocks_per_sm"   co-resident blocks of the batched kernel (0: autotune)
  *   "mixed.max_sweeps"      refinement sweeps per step (default 8)
- *   "mixed.eps_first"       inner FP32 tolerance of the first sweep (1e-4)
- *   "mixed.eps_next"        inner FP32 tolerance of later sweeps (3e-3)
+ *   "mixed.eps_first"       inner FP32 tolerance of the first sweep (3e-6)
+ *   "mixed.eps_next"        inner FP32 tolerance of later sweeps (1e-2)
  *   "mixed.blocked_rows"    rows of a block: 1 contiguous range, 0 interleaved, -1 tuned (default)
  *   "mixed.extrapolate"     initial guess of each step: 2 = 3u_n - 3u_{n-1} + u_{n-2} (default),
  *                           1 = 2u_n - u_{n-1}, 0 = u_n
