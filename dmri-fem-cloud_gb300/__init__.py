@@ -9,7 +9,7 @@ reference-named API (``api``), time profiles (``sequences``), synthetic
 geometries (``meshgen``) and the build recipe (``build``).
 """
 
-from . import _native, sequences, meshgen  # noqa: F401
+from . import _native, sequences, meshgen, meshfiles  # noqa: F401
 from .api import (  # noqa: F401
     Mesh, KrylovSolver, MRI_parameters, MyDomain, MRI_simulation, PostProcessing, simulate,
 )

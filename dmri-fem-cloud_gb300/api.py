@@ -25,6 +25,7 @@ conditions (``PeriodicDir != [0,0,0]``) are not part of this engine and raise.
 """
 
 import math
+import os
 import sys
 import time
 
@@ -32,6 +33,19 @@ import numpy as np
 
 from . import _native
 from . import sequences as seqs
+
+
+def _compact_markers(mk):
+    """Marker values renumbered to small non-negative integers, in increasing
+    order, each keeping its parity (phase = marker % 2 is preserved)."""
+    mk = np.asarray(mk, np.int64)
+    out = np.empty(len(mk), np.int32)
+    nxt = {0: 0, 1: 1}
+    for v in np.unique(mk):
+        par = int(v) % 2
+        out[mk == v] = nxt[par]
+        nxt[par] += 2
+    return out
 
 
 class Mesh:
@@ -45,6 +59,34 @@ class Mesh:
         if self.tets.ndim != 2 or self.tets.shape[1] != 4:
             raise ValueError("tets must be (n_cells, 4)")
         self.markers = None if markers is None else np.ascontiguousarray(markers, dtype=np.int32)
+
+    @classmethod
+    def read(cls, path, markers=None, compact_markers=False):
+        """Mesh from a gmsh ``.msh`` / DOLFIN ``.xml`` file (plain or ``.zip``).
+
+        Cell markers are the file's own (gmsh physical tags, DOLFIN domains);
+        ``markers`` may instead name a DOLFIN mesh-function file (the
+        ``pmk_*.xml`` of ``GetPartitionMarkers``, ``DmriFemLib.py:689``) or be an
+        array.  ``compact_markers`` renumbers the marker values to 0..k-1 in
+        increasing order while keeping each value's parity (so the reference's
+        phase = marker % 2 is unchanged)."""
+        from . import meshfiles
+        name = str(path)
+        stem = name[:-4] if name.endswith(".zip") else name
+        if stem.endswith(".msh"):
+            d = meshfiles.read_msh(path)
+        elif stem.endswith(".xml"):
+            d = meshfiles.read_dolfin_xml(path)
+        else:
+            raise ValueError("unknown mesh file type: %s (expected .msh or .xml, optionally .zip)" % name)
+        mk = d["markers"]
+        if isinstance(markers, (str, os.PathLike)):
+            mk = meshfiles.read_mesh_function(markers, len(d["tets"]))
+        elif markers is not None:
+            mk = np.asarray(markers, np.int32)
+        if mk is not None and compact_markers:
+            mk = _compact_markers(mk)
+        return cls(d["xyz"], d["tets"], mk)
 
     def num_vertices(self):
         return len(self.xyz)
