@@ -32,7 +32,7 @@ EXPORTS = [
     "bt_mesh_upload", "bt_mesh_info", "bt_set_coefficients", "bt_set_cell_diffusion",
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
-    "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi",
+    "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2",
 ]
 
 
@@ -89,6 +89,7 @@ def load(path=None):
         "bt_mesh_info": (C.c_int, [_P, C.POINTER(MeshInfo)]),
         "bt_set_coefficients": (C.c_int, [_P, _D, _D, _D]),
         "bt_set_cell_diffusion": (C.c_int, [_P, _D]),
+        "bt_set_cell_T2": (C.c_int, [_P, _D]),
         "bt_assemble": (C.c_int, [_P]),
         "bt_set_schedule": (C.c_int, [_P, _D, _D, C.c_int32, C.c_int32, C.c_double, C.c_double]),
         "bt_solve": (C.c_int, [_P, C.c_int32, _D, _D, _I32, _D, C.c_int32, C.c_double, C.c_int32,
@@ -169,6 +170,7 @@ class Context:
         self._check(self.lib.bt_mesh_upload(self.h, _dp(xyz), len(xyz), _ip(tets), len(tets), _ip(reg),
                                             int(n_regions), _ip(rc_arr)))
         self.n_vertices = len(xyz)
+        self.n_cells = len(tets)
         self.n_regions = int(n_regions)
         self.n_compartments = self.info()["n_compartments"]
 
@@ -192,6 +194,13 @@ class Context:
     def set_cell_diffusion(self, D_cell6):
         arr = None if D_cell6 is None else np.ascontiguousarray(D_cell6, dtype=np.float64)
         self._check(self.lib.bt_set_cell_diffusion(self.h, _dp(arr)))
+
+    def set_cell_T2(self, invT2_cell):
+        """Per-cell 1/T2 (None clears it)."""
+        arr = None if invT2_cell is None else np.ascontiguousarray(invT2_cell, dtype=np.float64)
+        if arr is not None and arr.shape != (self.n_cells,):
+            raise ValueError("invT2_cell must have one value per cell")
+        self._check(self.lib.bt_set_cell_T2(self.h, _dp(arr)))
 
     def assemble(self):
         self._check(self.lib.bt_assemble(self.h))

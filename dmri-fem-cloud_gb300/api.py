@@ -296,13 +296,22 @@ class MyDomain:
         """Upload + assemble once; re-assemble when coefficients change."""
         reg, nr, rc = self.regions()
         D = self.D if self.D is not None else 3e-3
-        T2 = np.broadcast_to(np.asarray(mri_para.T2, np.float64), (nr,))
-        iT2 = np.where(T2 >= 1e15, 0.0, 1.0 / T2)     # T2 = 1e16 means no decay
+        # T2: a scalar, one value per region, or one per cell (a DG0 field,
+        # T2_Relaxation.ipynb); T2 >= 1e15 means no decay (the reference's 1e16)
+        T2a = np.asarray(mri_para.T2, np.float64)
+        n_t = self.mymesh.num_cells()
+        iT2_cell = None
+        if T2a.ndim == 1 and T2a.size == n_t and n_t != nr:
+            iT2_cell = np.where(T2a >= 1e15, 0.0, 1.0 / T2a)
+            T2a = np.float64(1e16)
+        T2 = np.broadcast_to(T2a, (nr,))
+        iT2 = np.where(T2 >= 1e15, 0.0, 1.0 / T2)
         kp = np.asarray(self.kappa, np.float64)
         if kp.ndim == 0:
             kp = np.full((nr, nr), float(kp))
         Dr = np.broadcast_to(np.asarray(3e-3 if isinstance(D, str) else D, np.float64), (nr,)).copy()
-        key = (Dr.tobytes(), iT2.tobytes(), kp.tobytes(), None if self._D_cell is None else id(self._D_cell))
+        key = (Dr.tobytes(), iT2.tobytes(), kp.tobytes(), None if self._D_cell is None else id(self._D_cell),
+               None if iT2_cell is None else iT2_cell.tobytes())
         if self._ctx is None:
             self._ctx = _native.Context(self.device)
             self._ctx.mesh_upload(self.mymesh.xyz, self.mymesh.tets, reg, nr, rc)
@@ -310,6 +319,7 @@ class MyDomain:
         if self._state != key:
             self._ctx.set_coefficients(Dr, iT2, kp)
             self._ctx.set_cell_diffusion(self._D_cell)
+            self._ctx.set_cell_T2(iT2_cell)
             self._ctx.assemble()
             self._state = key
         return self._ctx

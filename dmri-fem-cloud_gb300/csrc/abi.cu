@@ -195,6 +195,28 @@ int bt_set_cell_diffusion(bt_ctx* ctx, const double* D_cell) {
     });
 }
 
+int bt_set_cell_T2(bt_ctx* ctx, const double* invT2_cell) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Mesh& m = ctx->mesh;
+        BT_REQUIRE(m.built, BT_ERR_STATE, "bt_set_cell_T2: no mesh");
+        use_device(ctx);
+        bt::Coeffs& c = ctx->coeffs;
+        if (!invT2_cell) {
+            c.invT2_cell.release();
+            c.has_cell_T2 = false;
+        } else {
+            for (int64_t i = 0; i < m.n_t; ++i)
+                BT_REQUIRE(std::isfinite(invT2_cell[i]) && invT2_cell[i] >= 0.0, BT_ERR_INVALID,
+                           "invT2_cell must be finite and >= 0");
+            c.invT2_cell.upload(invT2_cell, (size_t)m.n_t, ctx->stream);
+            BT_CUDA(cudaStreamSynchronize(ctx->stream));
+            c.has_cell_T2 = true;
+        }
+        ctx->mat.done = false;
+    });
+}
+
 int bt_assemble(bt_ctx* ctx) {
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {

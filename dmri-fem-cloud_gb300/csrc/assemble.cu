@@ -38,6 +38,7 @@ struct AsmArgs {
     const double* D_region;
     const double* D_cell;  // nullable, 6 per cell
     const double* invT2_region;
+    const double* invT2_cell;  // nullable, 1 per cell (overrides invT2_region)
     const double* kappa_pair;
     double *M, *K, *T, *R, *Jx, *Jy, *Jz, *w, *vw;
     int* status;
@@ -113,7 +114,7 @@ __global__ void k_assemble_colour(AsmArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) D[r][c] = (r == c) ? s : 0.0;
     }
-    const double iT2 = a.invT2_region[reg];
+    const double iT2 = a.invT2_cell ? a.invT2_cell[t] : a.invT2_region[reg];
     double DG[4][3];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -283,6 +284,7 @@ void assemble_all(bt_ctx* ctx) {
     a.D_region = cf.D_region;
     a.D_cell = cf.has_cell_D ? cf.D_cell.p : nullptr;
     a.invT2_region = cf.invT2_region;
+    a.invT2_cell = cf.has_cell_T2 ? cf.invT2_cell.p : nullptr;
     a.kappa_pair = cf.kappa_pair;
     a.M = A.M; a.K = A.K; a.T = A.T; a.R = A.R;
     a.Jx = A.Jx; a.Jy = A.Jy; a.Jz = A.Jz;

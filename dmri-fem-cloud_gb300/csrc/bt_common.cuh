@@ -130,8 +130,9 @@ struct Mesh {
 };
 
 struct Coeffs {
-    DevBuf<double> D_region, invT2_region, kappa_pair, D_cell;
+    DevBuf<double> D_region, invT2_region, kappa_pair, D_cell, invT2_cell;
     bool has_cell_D = false;
+    bool has_cell_T2 = false;
     bool set = false;
 };
 

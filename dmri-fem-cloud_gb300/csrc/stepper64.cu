@@ -718,6 +718,8 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
     cudaStream_t s = ctx->stream;
     BT_REQUIRE(!ctx->coeffs.has_cell_D, BT_ERR_STATE,
                "bt_adjoint: gradients are defined for per-region isotropic D (clear the per-cell tensor)");
+    BT_REQUIRE(!ctx->coeffs.has_cell_T2, BT_ERR_STATE,
+               "bt_adjoint: gradients are defined for per-region 1/T2 (clear the per-cell T2)");
     if (!ctx->s64) ctx->s64 = new Solver64();
     Solver64& W = *ctx->s64;
     prepare_fp64(ctx, W);

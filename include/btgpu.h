@@ -119,6 +119,11 @@ int bt_set_coefficients(bt_ctx* ctx, const double* D_region, const double* invT2
  * clears it (back to D_region). */
 int bt_set_cell_diffusion(bt_ctx* ctx, const double* D_cell);
 
+/* Optional per-cell relaxation: invT2_cell[n_cells] = 1/T2 per cell (a DG0 T2
+ * field, T2_Relaxation.ipynb; 0 = no decay), overriding invT2_region.  NULL
+ * clears it.  bt_adjoint rejects per-cell T2 (its gradients are per region). */
+int bt_set_cell_T2(bt_ctx* ctx, const double* invT2_cell);
+
 /* Assemble M, K, T, R, Jx, Jy, Jz and the signal weights on the device with the
  * coloured, atomic-free element kernel.  Replaces the FFC tabulate_tensor +
  * PETSc insertion behind assemble() (DmriFemLib.py:245,252,904-905). */

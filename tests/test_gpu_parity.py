@@ -96,6 +96,35 @@ def test_anisotropic_cell_tensor(pkg, lib):
     ctx.close()
 
 
+def test_cell_T2_field(pkg, lib):
+    """Per-cell 1/T2 (a DG0 T2 field): the T2 mass matrix and a signal against
+    the oracle with the same field; the adjoint refuses per-cell T2."""
+    xyz, tets, reg, D, iT2, kp = layered(pkg, n=6)
+    rng = np.random.default_rng(11)
+    iT2c = rng.uniform(0.0, 3e-5, size=len(tets))
+    ctx = make_ctx(pkg, xyz, tets, reg, 4, D, iT2, kp)
+    ctx.set_cell_T2(iT2c)
+    ctx.assemble()
+    sd = oracle.duplicated_system(xyz, tets, reg, D, iT2c, kp)
+    A = gpu_csr(ctx, ctx.matrix("T"))
+    assert abs(A - sd["T"]).max() <= MAT_RTOL * abs(sd["T"]).max()
+    p = pkg.sequences.pgse(10600, 43100)
+    fn, fo = pkg.sequences.profile_samples(p, 200.0)
+    ctx.set_schedule(fn, fo, 200.0)
+    q = pkg.sequences.b_to_q(2000.0, p.int4gb())
+    g = np.array([0.6, 0.0, 0.8])
+    got = ctx.solve([q], [g], precision=pkg.PRECISION_FP64, rtol=1e-13, max_iterations=20000)
+    ref = oracle.solve_duplicated(sd, oracle.PGSE(10600, 43100), q, g, 200.0)
+    assert abs(got["signal"][0] / got["S0"] - ref.normalized) <= 1e-9 * abs(ref.normalized)
+    with pytest.raises(pkg.BtError):
+        ctx.adjoint(q, g)
+    ctx.set_cell_T2(None)
+    ctx.assemble()
+    sd0 = oracle.duplicated_system(xyz, tets, reg, D, iT2, kp)
+    assert abs(gpu_csr(ctx, ctx.matrix("T")) - sd0["T"]).max() <= MAT_RTOL * abs(sd0["T"]).max()
+    ctx.close()
+
+
 def test_colouring_is_valid(pkg, lib):
     xyz, tets = pkg.meshgen.kuhn_box(-5, 5, 9)
     reg = pkg.meshgen.cylinder_regions(xyz, tets, [(0, 0)], [3.0])
