@@ -69,6 +69,7 @@ int bt_create(bt_ctx** out, int device) {
         BT_CUDA(cudaEventCreate(&ctx->ev0));
         BT_CUDA(cudaEventCreate(&ctx->ev1));
         BT_CUDA(cudaEventCreate(&ctx->ev2));
+        BT_CUDA(cudaEventCreate(&ctx->ev3));
     });
     if (rc != BT_OK) {
         bt_destroy(ctx);
@@ -88,6 +89,7 @@ int bt_destroy(bt_ctx* ctx) {
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+    if (ctx->ev3) cudaEventDestroy(ctx->ev3);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return BT_OK;

@@ -1475,24 +1475,13 @@ static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R
     return ms;
 }
 
-void solve_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q, const double* gdir,
-                       const int32_t* seq, double rtol, int32_t maxit, double* sig, bt_stats* st) {
+// Meshes that cannot fill the GPU alone, in one persistent launch (all on the
+// first context's stream).
+static void multi_launch_group(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q,
+                               const double* gdir, const int32_t* seq, double rtol, int32_t maxit, double* sig,
+                               bt_stats* st) {
     bt_ctx* c0 = ctxs[0];
     cudaStream_t s = c0->stream;
-    // every mesh's work goes on the first context's stream for this call
-    std::vector<cudaStream_t> saved(nm);
-    for (int m = 0; m < nm; ++m) {
-        BT_CUDA(cudaStreamSynchronize(ctxs[m]->stream));
-        saved[m] = ctxs[m]->stream;
-        ctxs[m]->stream = s;
-    }
-    struct Restore {
-        bt_ctx* const* c;
-        std::vector<cudaStream_t>& v;
-        ~Restore() {
-            for (size_t m = 0; m < v.size(); ++m) c[m]->stream = v[m];
-        }
-    } restore{ctxs, saved};
     std::vector<int> R(nm);
     std::vector<const double*> d_u0(nm, nullptr);
     std::vector<int64_t> off(nm + 1, 0);
@@ -1555,6 +1544,88 @@ void solve_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, con
         st->stepper_ms = ms;
         st->kernel_launches = 2 * nm + 1;
     }
+}
+
+static void add_stats(bt_stats* st, const bt_stats& a) {
+    if (!st) return;
+    st->steps = std::max(st->steps, a.steps);
+    st->max_iterations = std::max(st->max_iterations, a.max_iterations);
+    st->total_iterations += a.total_iterations;
+    st->refinements += a.refinements;
+    st->kernel_launches += a.kernel_launches;
+    st->stepper_ms += a.stepper_ms;
+    st->gpu_ms += a.gpu_ms;
+}
+
+// Several meshes: a mesh whose batch fills every SM by itself (at least one
+// warp-unit group of 8 per SM) runs alone on the whole GPU, back to back with the
+// other large ones; the remaining small meshes share one persistent launch, one
+// sub-grid each.  (A shared launch is capped at one block per SM, so a large
+// mesh gains nothing from sharing and loses half its blocks.)
+void solve_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q, const double* gdir,
+                       const int32_t* seq, double rtol, int32_t maxit, double* sig, bt_stats* st) {
+    bt_ctx* c0 = ctxs[0];
+    cudaStream_t s = c0->stream;
+    // every mesh's work goes on the first context's stream for this call
+    std::vector<cudaStream_t> saved(nm);
+    for (int m = 0; m < nm; ++m) {
+        BT_CUDA(cudaStreamSynchronize(ctxs[m]->stream));
+        saved[m] = ctxs[m]->stream;
+        ctxs[m]->stream = s;
+    }
+    struct Restore {
+        bt_ctx* const* c;
+        std::vector<cudaStream_t>& v;
+        ~Restore() {
+            for (size_t m = 0; m < v.size(); ++m) c[m]->stream = v[m];
+        }
+    } restore{ctxs, saved};
+    std::vector<int64_t> off(nm + 1, 0);
+    for (int m = 0; m < nm; ++m) off[m + 1] = off[m] + nsig[m];
+    std::vector<int> small, large;
+    for (int m = 0; m < nm; ++m) {
+        // warp-units of the batch: rows x slots / 64, whatever the lanes-per-row
+        const int64_t units = ctxs[m]->mesh.n_dofs * (int64_t)ceil_pow2(2 * nsig[m]) / 64;
+        (units / kWarpsB >= ctxs[m]->num_sms ? large : small).push_back(m);
+    }
+    if (small.size() == 1) {
+        large.push_back(small[0]);
+        small.clear();
+    }
+    reset_stats(st, 0, rtol);
+    BT_CUDA(cudaEventRecord(c0->ev3, s));
+    for (int m : large) {
+        bt_stats one{};
+        solve_mixed(ctxs[m], nsig[m], q + off[m], gdir + 3 * off[m], seq ? seq + off[m] : nullptr, nullptr, rtol,
+                    maxit, sig + off[m], nullptr, &one);
+        add_stats(st, one);
+    }
+    if (!small.empty()) {
+        std::vector<bt_ctx*> cs;
+        std::vector<int32_t> ns;
+        std::vector<double> qs, gs, out;
+        std::vector<int32_t> ss;
+        for (int m : small) {
+            cs.push_back(ctxs[m]);
+            ns.push_back(nsig[m]);
+            qs.insert(qs.end(), q + off[m], q + off[m + 1]);
+            gs.insert(gs.end(), gdir + 3 * off[m], gdir + 3 * off[m + 1]);
+            if (seq) ss.insert(ss.end(), seq + off[m], seq + off[m + 1]);
+        }
+        out.resize(qs.size());
+        bt_stats grp{};
+        multi_launch_group(cs.data(), (int32_t)cs.size(), ns.data(), qs.data(), gs.data(), seq ? ss.data() : nullptr,
+                           rtol, maxit, out.data(), &grp);
+        add_stats(st, grp);
+        size_t k = 0;
+        for (int m : small)
+            for (int32_t i = 0; i < nsig[m]; ++i) sig[off[m] + i] = out[k++];
+    }
+    BT_CUDA(cudaEventRecord(c0->ev2, s));
+    BT_CUDA(cudaEventSynchronize(c0->ev2));
+    float total = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&total, c0->ev3, c0->ev2));
+    if (st) st->gpu_ms = total;
 }
 
 void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u) {

@@ -168,7 +168,7 @@ struct bt_ctx {
     int32_t last_nsig = 0;
     int32_t last_precision = -1;
     std::vector<int32_t> last_iters;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     // tuning knobs (bt_set_option); negative = automatic
     int opt_mixed_lpr = -1;
     int opt_mixed_blocks_per_sm = -1;

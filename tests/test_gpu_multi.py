@@ -72,3 +72,21 @@ def test_multi_rejects_bad_calls(pkg, lib):
         pkg.solve_multi(ctxs, q, g, [[0], [5]])            # no such sequence row
     for c in ctxs + [fresh]:
         c.close()
+
+
+def test_large_and_small_meshes_together(pkg, lib):
+    """One mesh large enough to fill the GPU runs on its own, the small ones share
+    a launch; every signal still matches the FP64 path."""
+    big = pkg.meshgen.workload("cfg2", n=30)
+    small = pkg.meshgen.uneven_meshes(count=2, seed=5, nmin=6, nmax=8, cube=1.5)
+    meshes = [dict(xyz=big["xyz"], tets=big["tets"], region=big["region"], D=big["D"], kappa=big["kappa"])] + small
+    ctxs, int4 = contexts(pkg, meshes)
+    q = [[pkg.sequences.b_to_q(b, int4[0]) for b in (1000.0, 2000.0, 3000.0, 4000.0)]] * 3
+    g = [pkg.meshgen.fibonacci_directions(4)] * 3
+    out = pkg.solve_multi(ctxs, q, g, rtol=1e-9)
+    for m, ctx in enumerate(ctxs):
+        ref = ctx.solve(q[m], g[m], precision=pkg.PRECISION_FP64, rtol=1e-12)
+        rel = np.abs(out["signal"][m] - ref["signal"]) / np.abs(ref["signal"])
+        assert rel.max() <= MIX_RTOL, (m, rel.max())
+    for c in ctxs:
+        c.close()
