@@ -36,10 +36,7 @@ void use_device(bt_ctx* ctx) { BT_CUDA(cudaSetDevice(ctx->device)); }
 
 }  // namespace
 
-std::mutex& bt::persistent_kernel_mutex() {
-    static std::mutex mu;
-    return mu;
-}
+
 
 extern "C" {
 

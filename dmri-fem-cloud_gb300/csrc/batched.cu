@@ -396,7 +396,6 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
     constexpr int G = 32 / LPR;  // rows per warp-unit
     constexpr int C = 2 * LPR;   // RHS per warp-unit
     __shared__ float2 smem[kWarpsB * 64 * kNV > kMaxRhs * kNV ? kWarpsB * 64 * kNV : kMaxRhs * kNV];
-    __shared__ int s_flag;
     const int lane = threadIdx.x & 31;
     const int gw = bid * kWarpsB + (threadIdx.x >> 5);
     const int total_warps = nb * kWarpsB;
@@ -620,16 +619,14 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             bool act[2];
             int it = 0;
             while (true) {
-                // lane-local activity of its two RHS; grid decision via s_flag below
+                // lane-local activity of its two RHS; the block-wide OR is the same in every
+                // block (rr2 / rrs are grid-identical sums).  __syncthreads_or has barrier
+                // semantics and no shared flag: a shared flag reset by one thread for the
+                // next decision can race with a slow warp still reading the previous one.
 #pragma unroll
                 for (int j = 0; j < 2; ++j)
                     act[j] = (r0 + j < a.R) && rr2[j] > eps * eps * rrs[j] && rr2[j] > 0.09f * tolb2[j];
-                if (threadIdx.x == 0) s_flag = 0;
-                __syncthreads();
-                if (act[0] || act[1]) s_flag = 1;
-                __syncthreads();
-                // every block sees the same rr2/rrs (grid-identical sums), so s_flag is uniform
-                if (!s_flag) break;
+                if (!__syncthreads_or(act[0] || act[1])) break;
                 if (it >= a.maxit) {
                     if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
 #pragma unroll
@@ -863,11 +860,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             }
             // the lane's two slots are Re and Im of one signal: ||r||^2 = sum of both
             if (r0 < a.R && rr2[0] + rr2[1] > tolb2[0]) more = true;
-            if (threadIdx.x == 0) s_flag = 0;
-            __syncthreads();
-            if (more) s_flag = 1;
-            __syncthreads();
-            if (!s_flag) break;
+            if (!__syncthreads_or(more)) break;
             if (sweep >= a.max_sweeps) {
                 if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
                 if (bid == 0 && r0 < a.R && rr2[0] + rr2[1] > tolb2[0]) {
@@ -1207,7 +1200,6 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     const int nb = std::max(1, std::min(per_sm * ctx->num_sms, blocks_needed(ctx, R, lpr)));
     MixArgs a = prepare_batch(ctx, W, R, lpr, nb, blocked, n_steps, rtol, maxit, d_u0);
     void* args[] = {&a};
-    std::lock_guard<std::mutex> lock(persistent_kernel_mutex());
     BT_CUDA(cudaEventRecord(ctx->ev1, s));
     BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(nb), dim3(kThreadsB), args, 0, s));
     BT_CUDA(cudaEventRecord(ctx->ev2, s));
@@ -1445,10 +1437,9 @@ static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R
     int occ = 0;
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
     BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
-    // One block per SM in total: with two blocks per SM, blocks of different meshes
-    // share an SM, and in that arrangement the stepper was observed to stagnate
-    // non-deterministically (one block per SM never did).
-    const int total = c0->num_sms;
+    const int per_sm =
+        c0->opt_mixed_blocks_per_sm > 0 ? std::min(occ, c0->opt_mixed_blocks_per_sm) : std::min(occ, 2);
+    const int total = per_sm * c0->num_sms;
     const std::vector<int> nb = split_blocks(ctxs, nm, R, lpr, total);
     std::vector<MixArgs> args(nm);
     std::vector<int> first(nm + 1, 0);
@@ -1465,7 +1456,6 @@ static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R
     const int* pf = W0.mfirst.p;
     int nmi = nm;
     void* kargs[] = {&pa, &pf, &nmi};
-    std::lock_guard<std::mutex> lock(persistent_kernel_mutex());
     BT_CUDA(cudaEventRecord(c0->ev1, s));
     BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(first[nm]), dim3(kThreadsB), kargs, 0, s));
     BT_CUDA(cudaEventRecord(c0->ev2, s));
@@ -1557,11 +1547,11 @@ static void add_stats(bt_stats* st, const bt_stats& a) {
     st->gpu_ms += a.gpu_ms;
 }
 
-// Several meshes: a mesh whose batch fills every SM by itself (at least one
-// warp-unit group of 8 per SM) runs alone on the whole GPU, back to back with the
-// other large ones; the remaining small meshes share one persistent launch, one
-// sub-grid each.  (A shared launch is capped at one block per SM, so a large
-// mesh gains nothing from sharing and loses half its blocks.)
+// Several meshes: a mesh whose batch fills every co-resident block slot by itself
+// (two blocks of 8 warp-units per SM) runs alone on the whole GPU, back to back
+// with the other large ones; the remaining small meshes share one persistent
+// launch, one sub-grid each (a large mesh gains nothing from sharing the GPU's
+// blocks and would lose most of them).
 void solve_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q, const double* gdir,
                        const int32_t* seq, double rtol, int32_t maxit, double* sig, bt_stats* st) {
     bt_ctx* c0 = ctxs[0];
@@ -1586,7 +1576,7 @@ void solve_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, con
     for (int m = 0; m < nm; ++m) {
         // warp-units of the batch: rows x slots / 64, whatever the lanes-per-row
         const int64_t units = ctxs[m]->mesh.n_dofs * (int64_t)ceil_pow2(2 * nsig[m]) / 64;
-        (units / kWarpsB >= ctxs[m]->num_sms ? large : small).push_back(m);
+        (units / kWarpsB >= 2 * ctxs[m]->num_sms ? large : small).push_back(m);
     }
     if (small.size() == 1) {
         large.push_back(small[0]);

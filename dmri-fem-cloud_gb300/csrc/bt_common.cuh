@@ -4,8 +4,6 @@
 #pragma once
 
 #include <cuda_runtime.h>
-
-#include <mutex>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -201,9 +199,7 @@ void solve_mixed_multi(bt_ctx* const* ctxs, int32_t n_meshes, const int32_t* nsi
                        const double* gdir, const int32_t* seq, double rtol, int32_t maxit, double* sig,
                        bt_stats* st);
 void reset_tuning_mixed(bt_ctx* ctx);
-// Held from the launch of a persistent (grid-barrier) kernel until its stream has
-// drained: two such grids of this library never share the GPU's SMs.
-std::mutex& persistent_kernel_mutex();
+
 void free_solvers(bt_ctx* ctx);
 double device_sum(const double* d, int64_t n, cudaStream_t s);
 double device_dot(const double* a, const double* b, int64_t n, cudaStream_t s);

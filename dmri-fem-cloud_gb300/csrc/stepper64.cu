@@ -470,7 +470,6 @@ static float run_steps_fp64(bt_ctx* ctx, Solver64& W, const double* d_cn, const 
         BT_REQUIRE(n_steps >= 1 && (size_t)n_steps <= W.iters.n, BT_ERR_INVALID, "stepper: bad step count");
     }
     void* args[] = {&a};
-    std::lock_guard<std::mutex> lock(persistent_kernel_mutex());
     BT_CUDA(cudaEventRecord(ctx->ev1, s));
     BT_CUDA(cudaLaunchCooperativeKernel((const void*)k_step64, dim3(W.nblocks), dim3(kThreads64), args, 0, s));
     BT_CUDA(cudaEventRecord(ctx->ev2, s));

@@ -90,3 +90,56 @@ def test_large_and_small_meshes_together(pkg, lib):
         assert rel.max() <= MIX_RTOL, (m, rel.max())
     for c in ctxs:
         c.close()
+
+
+def test_colocated_grids_are_deterministic(pkg, lib):
+    """Blocks of different meshes on one SM (two blocks per SM) and two contexts
+    solving at the same time from two host threads: every run gives bitwise the
+    signals of the same solve run alone.  (A block-level decision once read a
+    shared flag that one thread could reset before a slow warp had read it; that
+    showed only when another grid's blocks shared the SM.)"""
+    import threading
+    meshes = pkg.meshgen.uneven_meshes(count=4, seed=3, nmin=6, nmax=14, cube=1.5)
+    pick = [meshes[1], meshes[3]]
+    ctxs, int4 = contexts(pkg, pick + pick)          # two copies of each mesh
+    rng = np.random.default_rng(7)
+    q, g, sq = [], [], []
+    for cnt in (8, 5):
+        d = rng.normal(size=(cnt, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        s = rng.integers(0, 2, size=cnt)
+        b = rng.uniform(500, 4000, size=cnt)
+        q.append([pkg.sequences.b_to_q(bb, int4[x]) for bb, x in zip(b, s)])
+        g.append(d)
+        sq.append(s)
+    q, g, sq = q + q, g + g, sq + sq
+    for c in ctxs:
+        c.set_option("mixed.lanes_per_row", 4)
+        c.set_option("mixed.blocks_per_sm", 2)
+    first = pkg.solve_multi(ctxs[:2], q[:2], g[:2], sq[:2], rtol=1e-9)["signal"]
+    for _ in range(3):
+        again = pkg.solve_multi(ctxs[:2], q[:2], g[:2], sq[:2], rtol=1e-9)["signal"]
+        assert all(np.array_equal(a, b) for a, b in zip(first, again))
+    for m in range(2):
+        ref = ctxs[m].solve(q[m], g[m], sq[m], precision=pkg.PRECISION_FP64, rtol=1e-12)["signal"]
+        assert np.max(np.abs(first[m] - ref) / np.abs(ref)) <= MIX_RTOL
+    # two host threads, two contexts of the larger mesh, solving concurrently
+    for c in (ctxs[1], ctxs[3]):
+        c.set_option("mixed.blocks_per_sm", 1)
+    alone = ctxs[1].solve(q[1], g[1], sq[1], precision=pkg.PRECISION_MIXED, rtol=1e-9)["signal"]
+    results, errors = {1: [], 3: []}, []
+
+    def work(i):
+        try:
+            for _ in range(3):
+                results[i].append(ctxs[i].solve(q[i], g[i], sq[i], precision=pkg.PRECISION_MIXED, rtol=1e-9)["signal"])
+        except Exception as e:          # reported below, after both threads ended
+            errors.append(e)
+
+    th = [threading.Thread(target=work, args=(i,)) for i in (1, 3)]
+    [t.start() for t in th]
+    [t.join() for t in th]
+    assert not errors, errors
+    assert all(np.array_equal(r, alone) for i in (1, 3) for r in results[i])
+    for c in ctxs:
+        c.close()
