@@ -22,6 +22,9 @@ to the host).
 512 signals (Fibonacci directions x b-values, PGSE and cos-OGSE) in one
 mixed-precision launch against the FP64 path on two of the same signals.
 
+``uneven`` runs 16 small meshes of uneven size in one persistent launch
+(bt_solve_multi) against one launch per mesh.
+
 ``--impl reference`` times the CPU restatement of the reference's solve path
 (two-field real system, Jacobi-BiCGSTAB rtol 1e-9 as GCloudDmriSolver.py
 ships it) with one process per host core, on a bounded sample of time steps.
@@ -301,6 +304,7 @@ def gpu_run(args):
         plain["max_rel_err_mixed_vs_fp64"] = float(np.max(np.abs(norm - n64) / np.abs(n64)))
 
     batched = batched_leg(args, pkg, stream, flush, peak, peak_src) if args.batched_signals > 0 else None
+    uneven = uneven_leg(args, pkg, stream, flush) if args.uneven_meshes > 0 else None
 
     # end to end through the public C-ABI from host buffers
     e2e_ms = []
@@ -343,6 +347,7 @@ def gpu_run(args):
             "roofline": roof,
             "plain_fp64": plain,
             "batched": batched,
+            "uneven": uneven,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "signals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
@@ -418,6 +423,57 @@ def batched_leg(args, pkg, stream, flush, peak, peak_src):
                          "note": "algorithmic bytes (bench.alg_bytes_mixed); working set larger than L2"}}
 
 
+def uneven_leg(args, pkg, stream, flush):
+    """Several meshes of uneven size in one persistent launch (bt_solve_multi):
+    `uneven_meshes` seeded boxes of 8^3 ... 24^3 Kuhn cubes of 1.5 um with
+    random z-cylinders (D 3e-3 / 2e-3, kappa U[1e-5,1e-4]), 4 b-values along one
+    direction each, PGSE; against one launch per mesh, and the largest mesh
+    against the FP64 path."""
+    import torch
+    meshes = pkg.meshgen.uneven_meshes(count=args.uneven_meshes, seed=0, nmin=8, nmax=24, cube=1.5)
+    p = pkg.sequences.pgse(10600, 43100)
+    fn, fo = pkg.sequences.profile_samples(p, 200.0)
+    qs = [pkg.sequences.b_to_q(b, p.int4gb()) for b in (1000.0, 2000.0, 3000.0, 4000.0)]
+    gs = [[0.36, 0.48, 0.8]] * 4
+    ctxs = []
+    for m in meshes:
+        c = pkg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+        c.set_stream(stream.cuda_stream)
+        c.mesh_upload(m["xyz"], m["tets"], m["region"], 2)
+        c.set_coefficients(m["D"], None, m["kappa"])
+        c.assemble()
+        c.set_schedule(fn, fo, 200.0)
+        ctxs.append(c)
+    n = len(ctxs)
+
+    def timed(fn_):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn_()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    pkg.solve_multi(ctxs, [qs] * n, [gs] * n, rtol=1e-9)                          # warm-up (tuning)
+    ms_one, out = timed(lambda: pkg.solve_multi(ctxs, [qs] * n, [gs] * n, rtol=1e-9))
+    for c in ctxs:
+        c.solve(qs, gs, precision=pkg.PRECISION_MIXED, rtol=1e-9)                # warm-up (tuning)
+    ms_sep, _ = timed(lambda: [c.solve(qs, gs, precision=pkg.PRECISION_MIXED, rtol=1e-9) for c in ctxs])
+    r64 = ctxs[-1].solve(qs, gs, precision=pkg.PRECISION_FP64, rtol=1e-12, max_iterations=20000)["signal"]
+    err = float(np.max(np.abs(out["signal"][-1] - r64) / np.abs(r64)))
+    dofs = [c.info()["n_dofs"] for c in ctxs]
+    for c in ctxs:
+        c.close()
+    nsig = 4 * n
+    return {"workload": "%d seeded cylinder boxes, 8^3..24^3 Kuhn cubes of 1.5 um (%d..%d dofs), 4 b-values each, "
+                        "PGSE 10600/43100 us" % (n, min(dofs), max(dofs)),
+            "signals": nsig, "value": nsig / (ms_one / 1e3), "unit": "signals/s", "ms": ms_one,
+            "separate_launches_value": nsig / (ms_sep / 1e3), "one_launch_over_separate": ms_sep / ms_one,
+            "max_rel_err_vs_fp64_largest_mesh": err}
+
+
 def reference_run(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -454,6 +510,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample-steps", type=int, default=8)
     ap.add_argument("--cpu-sample-steps-ref", type=int, default=6)
+    ap.add_argument("--uneven-meshes", type=int, default=16,
+                    help="meshes of the uneven multi-mesh leg (0: skip)")
     ap.add_argument("--batched-signals", type=int, default=64,
                     help="signals of the eight-cylinder 64^3 batched leg (0: skip)")
     args = ap.parse_args()
