@@ -648,9 +648,18 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 // a lane whose signal has converged in this sweep (or is padding) moves
                 // no data: its step length is zero and phase U restarts its vectors
                 const bool lane_active = act[0] || act[1];
-                for (int g = lane_active ? g0 : gend; g < gend; g += gstride) {
-                    const int row = g * G + slot;
-                    if (row >= a.n) continue;
+                // With 8 or more lanes per row the lanes of a row share its column indices
+                // and matrix values (one coalesced load, broadcast by shuffles), so all of a
+                // row's neighbour gathers are in flight at once; every lane of the warp then
+                // runs the same iterations (rows past the end are clamped, converged lanes
+                // skip their own gathers and stores).
+                constexpr bool kShared = (LPR >= 8);
+                for (int g = (kShared || lane_active) ? g0 : gend; g < gend; g += gstride) {
+                    const int row_raw = g * G + slot;
+                    if (!kShared && row_raw >= a.n) continue;
+                    const bool row_ok = row_raw < a.n;
+                    const int row = row_ok ? row_raw : a.n - 1;
+                    const bool mine = row_ok && lane_active;   // this lane updates its slots
                     float2 sA[2], sx[2], sy[2], sz[2];
 #pragma unroll
                     for (int j = 0; j < 2; ++j) sA[j] = sx[j] = sy[j] = sz[j] = make_float2(0.f, 0.f);
@@ -666,24 +675,61 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                         }
                     };
                     const size_t vi = (size_t)row * Rp4 + c4;
-                    const float4 po = a.p[vi], qo = a.q[vi];
-                    // eight independent neighbour gathers in flight per lane; the tail of
-                    // a row is predicated (a missing entry reads the own row times zero)
-                    for (int e = e0; e < e1; e += 8) {
-                        int cc[8];
-                        float4 mm[8], zz[8];
+                    const float4 f4z = make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float4 po = mine ? a.p[vi] : f4z, qo = mine ? a.q[vi] : f4z;
+                    if constexpr (kShared) {
+                        // windows of 16 entries: lane gl of the row's group loads entries gl,
+                        // gl + LPR, ... of the window, then 16 gathers go out together
+                        constexpr int W = 16;
+                        constexpr int K = (W + LPR - 1) / LPR;
+                        const int gl = lane % LPR;
+                        const int nn = e1 - e0;
+                        const int nmax = __reduce_max_sync(0xffffffffu, nn);
+                        for (int off = 0; off < nmax; off += W) {
+                            int my_c[K];
+                            float4 my_m[K];
 #pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            const bool ok = e + u < e1;
-                            cc[u] = ok ? a.col[e + u] : row;
-                            mm[u] = ok ? a.mA[e + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+                            for (int k = 0; k < K; ++k) {
+                                const int u = gl + k * LPR;
+                                const bool ok = u < W && off + u < nn;
+                                my_c[k] = ok ? a.col[e0 + off + u] : row;
+                                my_m[k] = ok ? a.mA[e0 + off + u] : f4z;
+                            }
+                            float4 zz[W];
+#pragma unroll
+                            for (int u = 0; u < W; ++u) {
+                                const int c = __shfl_sync(0xffffffffu, my_c[u / LPR], u % LPR, LPR);
+                                zz[u] = mine ? a.z[(size_t)c * Rp4 + c4] : f4z;
+                            }
+#pragma unroll
+                            for (int u = 0; u < W; ++u) {
+                                float4 m;
+                                m.x = __shfl_sync(0xffffffffu, my_m[u / LPR].x, u % LPR, LPR);
+                                m.y = __shfl_sync(0xffffffffu, my_m[u / LPR].y, u % LPR, LPR);
+                                m.z = __shfl_sync(0xffffffffu, my_m[u / LPR].z, u % LPR, LPR);
+                                m.w = __shfl_sync(0xffffffffu, my_m[u / LPR].w, u % LPR, LPR);
+                                acc_entry(m, zz[u]);
+                            }
                         }
+                    } else {
+                        // eight independent neighbour gathers in flight per lane; the tail of
+                        // a row is predicated (a missing entry reads the own row times zero)
+                        for (int e = e0; e < e1; e += 8) {
+                            int cc[8];
+                            float4 mm[8], zz[8];
 #pragma unroll
-                        for (int u = 0; u < 8; ++u) zz[u] = a.z[(size_t)cc[u] * Rp4 + c4];
+                            for (int u = 0; u < 8; ++u) {
+                                const bool ok = e + u < e1;
+                                cc[u] = ok ? a.col[e + u] : row;
+                                mm[u] = ok ? a.mA[e + u] : f4z;
+                            }
 #pragma unroll
-                        for (int u = 0; u < 8; ++u) acc_entry(mm[u], zz[u]);
+                            for (int u = 0; u < 8; ++u) zz[u] = a.z[(size_t)cc[u] * Rp4 + c4];
+#pragma unroll
+                            for (int u = 0; u < 8; ++u) acc_entry(mm[u], zz[u]);
+                        }
                     }
-                    const float4 zo = a.z[vi];
+                    const float4 zo = mine ? a.z[vi] : f4z;
                     const float zov[4] = {zo.x, zo.y, zo.z, zo.w}, pov[4] = {po.x, po.y, po.z, po.w},
                                 qov[4] = {qo.x, qo.y, qo.z, qo.w};
                     float pn[4], qn[4];
@@ -699,11 +745,15 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                         qn[2 * j] = wv.x + bq.x;
                         qn[2 * j + 1] = wv.y + bq.y;
                         const float2 pq = cmulf(make_float2(pn[2 * j], pn[2 * j + 1]), make_float2(qn[2 * j], qn[2 * j + 1]));
-                        kadd(mu[j][0], pq.x);
-                        kadd(mu[j][1], pq.y);
+                        if (mine) {
+                            kadd(mu[j][0], pq.x);
+                            kadd(mu[j][1], pq.y);
+                        }
                     }
-                    a.p[vi] = make_float4(pn[0], pn[1], pn[2], pn[3]);
-                    a.q[vi] = make_float4(qn[0], qn[1], qn[2], qn[3]);
+                    if (mine) {
+                        a.p[vi] = make_float4(pn[0], pn[1], pn[2], pn[3]);
+                        a.q[vi] = make_float4(qn[0], qn[1], qn[2], qn[3]);
+                    }
                 }
                 float ms[2][kNV];
                 BT_REDUCE(mu, ms);
