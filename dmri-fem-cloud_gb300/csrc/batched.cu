@@ -772,12 +772,8 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 for (int j = 0; j < 2; ++j)
 #pragma unroll
                     for (int k = 0; k < kNV; ++k) rb[j][k] = KF{0.0f, 0.0f};
-                for (int g = lane_active ? g0 : gend; g < gend; g += gstride) {
-                    const int row = g * G + slot;
-                    if (row >= a.n) continue;
-                    const size_t vi = (size_t)row * Rp4 + c4;
-                    const float4 pv = a.p[vi], qv = a.q[vi], dv = a.dv[dsel][vi], rv = a.ri[vi];
-                    const float4 dgr = a.dg[row];
+                auto phase_b_row = [&](size_t vi, const float4 pv, const float4 qv, const float4 dv, const float4 rv,
+                                       const float4 dgr) {
                     const float pvv[4] = {pv.x, pv.y, pv.z, pv.w}, qvv[4] = {qv.x, qv.y, qv.z, qv.w};
                     float dn[4] = {dv.x, dv.y, dv.z, dv.w}, rn[4] = {rv.x, rv.y, rv.z, rv.w}, zn[4];
 #pragma unroll
@@ -801,6 +797,22 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                     a.dv[dsel][vi] = make_float4(dn[0], dn[1], dn[2], dn[3]);
                     a.ri[vi] = make_float4(rn[0], rn[1], rn[2], rn[3]);
                     a.z[vi] = make_float4(zn[0], zn[1], zn[2], zn[3]);
+                };
+                // two rows per pass: both rows' loads are in flight together (same
+                // accumulation order as one row at a time)
+                for (int g = lane_active ? g0 : gend; g < gend; g += 2 * gstride) {
+                    const int rowA = g * G + slot, g2 = g + gstride, rowB = g2 * G + slot;
+                    const bool okA = rowA < a.n, okB = g2 < gend && rowB < a.n;
+                    const size_t viA = (size_t)(okA ? rowA : 0) * Rp4 + c4, viB = (size_t)(okB ? rowB : 0) * Rp4 + c4;
+                    const float4 f4z = make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float4 pA = okA ? a.p[viA] : f4z, qA = okA ? a.q[viA] : f4z;
+                    const float4 dA = okA ? a.dv[dsel][viA] : f4z, rA = okA ? a.ri[viA] : f4z;
+                    const float4 gA = okA ? a.dg[rowA] : f4z;
+                    const float4 pB = okB ? a.p[viB] : f4z, qB = okB ? a.q[viB] : f4z;
+                    const float4 dB = okB ? a.dv[dsel][viB] : f4z, rB = okB ? a.ri[viB] : f4z;
+                    const float4 gB = okB ? a.dg[rowB] : f4z;
+                    if (okA) phase_b_row(viA, pA, qA, dA, rA, gA);
+                    if (okB) phase_b_row(viB, pB, qB, dB, rB, gB);
                 }
                 float rbs[2][kNV];
                 BT_REDUCE(rb, rbs);
