@@ -474,6 +474,37 @@ def uneven_leg(args, pkg, stream, flush):
             "max_rel_err_vs_fp64_largest_mesh": err}
 
 
+def batched_profile(args):
+    """One short launch for a profiler: the batched leg's 64 signals on the
+    eight-cylinder 64^3 workload, schedule cut to `batched_profile` steps inside
+    the first gradient pulse, geometry fixed (lanes-per-row 32, two blocks per
+    SM, interleaved rows) so that no autotuner trial runs first."""
+    pkg = importlib.import_module(PKG)
+    pkg._native.load(pkg.build())
+    w = pkg.meshgen.workload("cfg3")
+    n = args.batched_profile
+    fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in w["profiles"]])
+    fn, fo = np.array(fns)[:, 20:20 + n], np.array(fos)[:, 20:20 + n]
+    int4 = [p.int4gb() for p in w["profiles"]]
+    sig = w["signals"]
+    sel = [sig[i] for i in np.linspace(0, len(sig) - 1, args.batched_signals).astype(int)]
+    q = np.array([pkg.sequences.b_to_q(b, int4[pi]) for b, _, pi in sel])
+    g = np.array([gd for _, gd, _ in sel], np.float64)
+    g /= np.linalg.norm(g, axis=1, keepdims=True)
+    pidx = np.array([pi for _, _, pi in sel], np.int32)
+    ctx = pkg.Context(0)
+    ctx.mesh_upload(w["xyz"], w["tets"], w["region"], w["n_regions"], None)
+    ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
+    ctx.assemble()
+    ctx.set_schedule(fn, fo, w["dt"])
+    for key, val in (("mixed.lanes_per_row", 32), ("mixed.blocks_per_sm", 2), ("mixed.blocked_rows", 0)):
+        ctx.set_option(key, val)
+    st = ctx.solve(q, g, pidx, None, pkg.PRECISION_MIXED, 1e-9, args.maxit)["stats"]
+    print(json.dumps({"batched_profile_steps": st["steps"], "stepper_ms": st["stepper_ms"],
+                      "inner_iterations": st["total_iterations"] / len(q), "refinements": st["refinements"]}))
+    ctx.close()
+
+
 def reference_run(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -510,6 +541,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample-steps", type=int, default=8)
     ap.add_argument("--cpu-sample-steps-ref", type=int, default=6)
+    ap.add_argument("--batched-profile", type=int, default=0,
+                    help="only one short batched launch of this many steps, for a profiler")
     ap.add_argument("--uneven-meshes", type=int, default=16,
                     help="meshes of the uneven multi-mesh leg (0: skip)")
     ap.add_argument("--batched-signals", type=int, default=64,
@@ -519,7 +552,9 @@ def main():
     args.warmup_e2e = 0
     args.warmup_ref = 0
     args.ref_steps = max(1, min(args.steps, 3))
-    if args.impl == "reference":
+    if args.batched_profile > 0:
+        batched_profile(args)
+    elif args.impl == "reference":
         reference_run(args)
     else:
         gpu_run(args)
