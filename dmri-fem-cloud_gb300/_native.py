@@ -32,7 +32,7 @@ EXPORTS = [
     "bt_mesh_upload", "bt_mesh_info", "bt_set_coefficients", "bt_set_cell_diffusion",
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
-    "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2",
+    "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
 ]
 
 
@@ -104,6 +104,8 @@ def load(path=None):
         "bt_signal_noalloc": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
         "bt_adjoint": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_double, C.c_int32, C.c_int32,
                                  _D, _D, _D, _D, C.POINTER(Stats)]),
+        "bt_tangent": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                 C.c_int32, _D, _D, C.POINTER(Stats)]),
         "bt_solve_multi": (C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _D, _I32, C.c_double, C.c_int32,
                                      _D, _D, C.POINTER(Stats)]),
     }
@@ -247,6 +249,18 @@ class Context:
                                         C.byref(st)))
         return {"signal": float(sig[0]), "dD": dD, "dinvT2": dT, "dkappa": dK.reshape(nr, nr),
                 "stats": st.as_dict()}
+
+    def tangent(self, q, gdir, param, i, j=0, sequence=0, u0=None, rtol=1e-13, max_iterations=5000):
+        """Signal and d(signal)/d(param) by a tangent-linear FP64 run; param is
+        "D" or "invT2" (region i) or "kappa" (region pair i, j)."""
+        kinds = {"D": 0, "invT2": 1, "kappa": 2}
+        g = np.ascontiguousarray(np.asarray(gdir, np.float64).reshape(3))
+        u = None if u0 is None else np.ascontiguousarray(np.asarray(u0, np.float64).reshape(self.n_vertices))
+        sig, d = np.zeros(1), np.zeros(1)
+        st = Stats()
+        self._check(self.lib.bt_tangent(self.h, float(q), _dp(g), int(sequence), _dp(u), kinds[param], int(i), int(j),
+                                        float(rtol), int(max_iterations), _dp(sig), _dp(d), C.byref(st)))
+        return {"signal": float(sig[0]), "d": float(d[0]), "stats": st.as_dict()}
 
     def csr(self):
         inf = self.info()

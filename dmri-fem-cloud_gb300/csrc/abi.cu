@@ -335,6 +335,26 @@ int bt_solve_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_s
     });
 }
 
+int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0, int32_t param,
+               int32_t i, int32_t j, double rtol, int32_t max_iterations, double* signal_out, double* dsignal_out,
+               bt_stats* stats) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_tangent: mesh not assembled");
+        BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_tangent: no schedule");
+        BT_REQUIRE(gdir && signal_out && dsignal_out, BT_ERR_INVALID, "bt_tangent: bad arguments");
+        BT_REQUIRE(std::isfinite(q) && std::isfinite(gdir[0]) && std::isfinite(gdir[1]) && std::isfinite(gdir[2]),
+                   BT_ERR_INVALID, "bt_tangent: q and gdir must be finite");
+        BT_REQUIRE(sequence >= 0 && sequence < ctx->sched.n_seq, BT_ERR_INVALID, "bt_tangent: bad sequence");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_tangent: rtol must be > 0 and max_iterations >= 1");
+        use_device(ctx);
+        ctx->last_precision = -1;
+        bt::tangent_fp64(ctx, q, gdir, sequence, u0, param, i, j, rtol, max_iterations, signal_out, dsignal_out,
+                         stats);   // the stepper now holds the tangent state: no solution to report
+    });
+}
+
 int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0, double rtol,
                int32_t max_iterations, int32_t checkpoint_stride, double* signal_out, double* dS_dD,
                double* dS_dinvT2, double* dS_dkappa, bt_stats* stats) {

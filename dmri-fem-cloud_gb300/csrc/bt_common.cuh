@@ -195,6 +195,8 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
                   bt_stats* st);
 void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u);
+void tangent_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const double* u0, int32_t kind, int32_t ri,
+                  int32_t rj, double rtol, int32_t maxit, double* sig, double* dsig, bt_stats* st);
 void solve_mixed_multi(bt_ctx* const* ctxs, int32_t n_meshes, const int32_t* nsig, const double* q,
                        const double* gdir, const int32_t* seq, double rtol, int32_t maxit, double* sig,
                        bt_stats* st);

@@ -90,6 +90,7 @@ struct StepArgs {
     int32_t extrapolate;
     double rtol2;
     const double* __restrict__ rhs_vec;  // nullable: right-hand side b = rhs_vec (real) for step 0
+    const double2* __restrict__ extra;   // nullable: extra[step * n_pad + i] added to b at every step
     double2* save;                       // nullable: state after step s saved to save[(s+1)/save_every - 1]
     int32_t save_every;
     int64_t n_pad;
@@ -173,8 +174,13 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 tJ.x = fma(m.y, vj.x, tJ.x); tJ.y = fma(m.y, vj.y, tJ.y);
             }
             const int64_t i = (int64_t)s * 32 + lane;
-            const double2 b = (a.rhs_vec && step == 0) ? make_double2(a.rhs_vec[i], 0.0)
-                                                       : make_double2(fma(co, sJ.y, sB.x), fma(-co, sJ.x, sB.y));
+            double2 b = (a.rhs_vec && step == 0) ? make_double2(a.rhs_vec[i], 0.0)
+                                                 : make_double2(fma(co, sJ.y, sB.x), fma(-co, sJ.x, sB.y));
+            if (a.extra) {
+                const double2 ex2 = a.extra[(int64_t)step * a.n_pad + i];
+                b.x += ex2.x;
+                b.y += ex2.y;
+            }
             // A x0 with x0 = 2 u_n - u_{n-1} (or u_n)
             const double ex = (a.extrapolate && !(a.rhs_vec && step == 0)) ? 1.0 : 0.0;
             const double2 gA = make_double2(sA.x + ex * (sA.x - tA.x), sA.y + ex * (sA.y - tA.y));
@@ -438,7 +444,7 @@ static void pack_signal_fp64(bt_ctx* ctx, Solver64& W, const double* gdir, const
 static float run_steps_fp64(bt_ctx* ctx, Solver64& W, const double* d_cn, const double* d_co, int n_steps,
                             bool extrapolate, const double* rhs_vec, double2* save, int save_every, double rtol,
                             int maxit, std::vector<int32_t>* iters_out, std::vector<double>* relres_out,
-                            double* out_sig) {
+                            double* out_sig, const double2* extra = nullptr) {
     Mesh& m = ctx->mesh;
     cudaStream_t s = ctx->stream;
     W.bar.zero(s);
@@ -457,6 +463,7 @@ static float run_steps_fp64(bt_ctx* ctx, Solver64& W, const double* d_cn, const 
     a.extrapolate = extrapolate ? 1 : 0;
     a.rtol2 = rtol * rtol;
     a.rhs_vec = rhs_vec;
+    a.extra = extra;
     a.save = save;
     a.save_every = save_every > 0 ? save_every : 1;
     a.n_pad = W.n_pad;
@@ -860,6 +867,128 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
         st->kernel_launches = 0;
         st->gpu_ms = total;
         st->stepper_ms = ms;
+    }
+}
+
+}  // namespace bt
+
+namespace bt {
+
+// extra[n][row] = -S_xi (theta u_{n+1} + (1-theta) u_n) for every step n: the
+// forcing of the tangent-linear recursion (CSR rows = stepper rows).
+__global__ void k_tl_forcing(int64_t n_dofs, int64_t n_pad, int32_t n_steps, const int32_t* __restrict__ row_ptr,
+                             const int32_t* __restrict__ col, const double* __restrict__ sxi,
+                             const double2* __restrict__ states, double theta, double2* __restrict__ extra) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)n_steps * n_pad) return;
+    const int64_t n = t / n_pad, i = t % n_pad;
+    double2 y = make_double2(0.0, 0.0);
+    if (i < n_dofs) {
+        const double2* un = states + n * n_pad;
+        const double2* u1 = states + (n + 1) * n_pad;
+        for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+            const int c = col[e];
+            const double s = sxi[e];
+            y.x = fma(s, theta * u1[c].x + (1.0 - theta) * un[c].x, y.x);
+            y.y = fma(s, theta * u1[c].y + (1.0 - theta) * un[c].y, y.y);
+        }
+    }
+    extra[t] = make_double2(-y.x, -y.y);
+}
+
+// Tangent-linear FP64 run for one parameter xi (kind 0: D of region i, 1: 1/T2 of
+// region i, 2: kappa of the region pair (i, j)):
+//   A_n v_{n+1} = B_n v_n - (dS/dxi) (theta u_{n+1} + (1 - theta) u_n),   v_0 = 0,
+// dSig/dxi = sum w Re(v_N).  dS/dxi is assembled with indicator coefficients into
+// scratch matrices (the system's matrices and coefficients are untouched); the
+// forward states are all kept on the device ((N+1) x n_pad complex values).
+void tangent_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const double* u0, int32_t kind, int32_t ri,
+                  int32_t rj, double rtol, int32_t maxit, double* sig, double* dsig, bt_stats* st) {
+    Mesh& m = ctx->mesh;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    BT_REQUIRE(!ctx->coeffs.has_cell_D && !ctx->coeffs.has_cell_T2, BT_ERR_STATE,
+               "bt_tangent: derivatives are defined for per-region coefficients (clear per-cell D / T2)");
+    const int nr = m.n_regions;
+    BT_REQUIRE(kind >= 0 && kind <= 2 && ri >= 0 && ri < nr && (kind != 2 || (rj >= 0 && rj < nr && rj != ri)),
+               BT_ERR_INVALID, "bt_tangent: bad parameter");
+    // dS/dxi with indicator coefficients, into scratch matrices
+    std::vector<double> eD(nr, 0.0), eT(nr, 0.0), eK((size_t)nr * nr, 0.0);
+    if (kind == 0) eD[ri] = 1.0;
+    if (kind == 1) eT[ri] = 1.0;
+    if (kind == 2) eK[(size_t)ri * nr + rj] = eK[(size_t)rj * nr + ri] = 1.0;
+    Coeffs ind;
+    ind.D_region.upload(eD.data(), nr, s);
+    ind.invT2_region.upload(eT.data(), nr, s);
+    ind.kappa_pair.upload(eK.data(), (size_t)nr * nr, s);
+    ind.set = true;
+    Assembled scratch;
+    std::swap(ctx->mat, scratch);
+    std::swap(ctx->coeffs, ind);
+    try {
+        assemble_all(ctx);
+    } catch (...) {
+        std::swap(ctx->mat, scratch);
+        std::swap(ctx->coeffs, ind);
+        throw;
+    }
+    std::swap(ctx->mat, scratch);
+    std::swap(ctx->coeffs, ind);
+    const double* sxi = (kind == 0) ? scratch.K.p : (kind == 1) ? scratch.T.p : scratch.R.p;
+
+    if (!ctx->s64) ctx->s64 = new Solver64();
+    Solver64& W = *ctx->s64;
+    prepare_fp64(ctx, W);
+    const int N = S.n_steps;
+    DevBuf<double> d_u0;
+    if (u0) d_u0.upload(u0, m.n_v, s);
+    std::vector<double> hcn, hco, hout(kRed);
+    schedule_row(S, seq, q, hcn, hco);
+    DevBuf<double> d_cn, d_co;
+    d_cn.upload(hcn.data(), N, s);
+    d_co.upload(hco.data(), N, s);
+    pack_signal_fp64(ctx, W, gdir, u0 ? d_u0.p : nullptr);
+    const size_t vb = (size_t)W.n_pad * sizeof(double2);
+    DevBuf<double2> states, extra;
+    states.alloc((size_t)(N + 1) * W.n_pad);
+    extra.alloc((size_t)N * W.n_pad);
+    std::vector<int32_t> hit1, hit2;
+    BT_CUDA(cudaEventRecord(ctx->ev0, s));
+    BT_CUDA(cudaMemcpyAsync(states.p, W.u[0].p, vb, cudaMemcpyDeviceToDevice, s));
+    float ms = run_steps_fp64(ctx, W, d_cn, d_co, N, ctx->opt_fp64_extrapolate != 0, nullptr, states.p + W.n_pad, 1,
+                              rtol, maxit, &hit1, nullptr, hout.data());
+    *sig = hout[0];
+    const int64_t total = (int64_t)N * W.n_pad;
+    k_tl_forcing<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(m.n_dofs, W.n_pad, N, m.row_ptr, m.col, sxi,
+                                                                  states.p, S.theta, extra.p);
+    BT_CUDA(cudaGetLastError());
+    // v_0 = 0 (also the extrapolation's previous level)
+    for (int k = 0; k < 3; ++k) BT_CUDA(cudaMemsetAsync(W.u[k].p, 0, vb, s));
+    ms += run_steps_fp64(ctx, W, d_cn, d_co, N, ctx->opt_fp64_extrapolate != 0, nullptr, nullptr, 1, rtol, maxit,
+                         &hit2, nullptr, hout.data(), extra.p);
+    *dsig = hout[0];
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    BT_CUDA(cudaEventSynchronize(ctx->ev2));
+    if (st) {
+        st->steps = N;
+        st->max_iterations = 0;
+        st->total_iterations = 0;
+        for (int32_t x : hit1) {
+            st->total_iterations += x;
+            st->max_iterations = std::max(st->max_iterations, x);
+        }
+        for (int32_t x : hit2) {
+            st->total_iterations += x;
+            st->max_iterations = std::max(st->max_iterations, x);
+        }
+        st->max_rel_residual = rtol;
+        st->refinements = 0;
+        st->graph_launches = 0;
+        st->kernel_launches = 3;
+        st->stepper_ms = ms;
+        float total_ms = 0.0f;
+        BT_CUDA(cudaEventElapsedTime(&total_ms, ctx->ev0, ctx->ev2));
+        st->gpu_ms = total_ms;
     }
 }
 

@@ -185,6 +185,20 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
                double* signal_out, double* dS_dD, double* dS_dinvT2, double* dS_dkappa,
                bt_stats* stats);
 
+/* Tangent-linear FP64 run: the signal and its derivative with respect to one
+ * coefficient, param = BT_PARAM_D (D of region i), BT_PARAM_INVT2 (1/T2 of
+ * region i) or BT_PARAM_KAPPA (permeability of the region pair (i, j)), by the
+ * forward-mode recursion A_n v_{n+1} = B_n v_n - (dS/dparam)(theta u_{n+1} +
+ * (1-theta) u_n), v_0 = 0.  A check of bt_adjoint (the two agree to solver
+ * precision); keeps all forward states on the device.  No counterpart in the
+ * reference (its derivatives would be finite differences). */
+#define BT_PARAM_D 0
+#define BT_PARAM_INVT2 1
+#define BT_PARAM_KAPPA 2
+int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0,
+               int32_t param, int32_t i, int32_t j, double rtol, int32_t max_iterations,
+               double* signal_out, double* dsignal_out, bt_stats* stats);
+
 /* Tuning knobs (no counterpart in the reference).  Keys:
  *   "mixed.lanes_per_row"   1,2,4,...,32 (0: autotune, the default)
  *   "mixed.blocks_per_sm"   co-resident blocks of the batched kernel (0: autotune)

@@ -1,6 +1,7 @@
 """GPU: discrete-adjoint gradients of the FP64 solve (bt_adjoint) against
 central finite differences with a 1e-6 relative step, of the GPU forward and of
-the CPU oracle.  Tolerance: 1e-5 relative to the gradient's scale."""
+the CPU oracle (tolerance 1e-5 relative to the gradient's scale), and against
+the FP64 tangent-linear run (bt_tangent, 1e-8)."""
 
 import numpy as np
 import pytest
@@ -114,4 +115,26 @@ def test_checkpoint_stride_invariance_and_autograd(pkg, lib):
     assert abs(float(s.detach()) - a["signal"] / S0) <= 1e-12
     assert np.allclose(Dt.grad.numpy(), a["dD"] / S0, rtol=1e-9, atol=0)
     assert np.allclose(Kt.grad.numpy(), a["dkappa"] / S0, rtol=1e-9, atol=0)
+    ctx.close()
+
+
+def test_tangent_linear_matches_adjoint(pkg, lib):
+    """The FP64 tangent-linear run (forward mode, one parameter at a time) and the
+    discrete adjoint give the same derivatives: both are exact derivatives of the
+    discrete solve, so they agree to solver precision (1e-8 relative)."""
+    xyz, tets, reg, D, invT2, kp = layered_case(pkg, n=6)
+    ctx, q = make(pkg, xyz, tets, reg, D, invT2, kp)
+    adj = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000)
+    checks = [("D", r, 0, adj["dD"][r]) for r in range(4)]
+    checks += [("invT2", r, 0, adj["dinvT2"][r]) for r in range(4)]
+    checks += [("kappa", i, j, adj["dkappa"][i, j]) for i, j in ((0, 1), (1, 2), (2, 3))]
+    scale = {"D": np.max(np.abs(adj["dD"])), "invT2": np.max(np.abs(adj["dinvT2"])),
+             "kappa": np.max(np.abs(adj["dkappa"]))}
+    for name, i, j, ref in checks:
+        t = ctx.tangent(q, G, name, i, j, rtol=1e-14, max_iterations=20000)
+        assert abs(t["signal"] - adj["signal"]) <= 1e-12 * abs(adj["signal"])
+        assert abs(t["d"] - ref) <= 1e-8 * scale[name], (name, i, j, t["d"], ref)
+    # assembled matrices are untouched by the indicator assembly
+    again = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000)
+    assert again["signal"] == adj["signal"]
     ctx.close()
