@@ -168,13 +168,14 @@ def cpu_baseline(name, steps, workers):
     integrate `steps` of the 270 steps of one signal; throughput is scaled to
     whole signals."""
     total_steps = 270
+    # one thread per worker process: BLAS / OpenMP pools would oversubscribe the
+    # cores (the variables are read when a spawned worker loads numpy)
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS"):
+        os.environ[var] = "1"
     t0 = time.perf_counter()
-    if workers == 1:
-        res = [_cpu_sample_worker((name, steps, 0))]
-    else:
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(workers) as pool:
-            res = pool.map(_cpu_sample_worker, [(name, steps, i) for i in range(workers)])
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        res = pool.map(_cpu_sample_worker, [(name, steps, i) for i in range(workers)])
     wall = time.perf_counter() - t0
     per_step = max(e / s for e, s in res)      # slowest worker's solve time per step
     sig_per_s = workers / (per_step * total_steps)
