@@ -131,7 +131,7 @@ struct MixArgs {
     float rtol;
     float eps_first;
     float eps_next;
-    int32_t two_stage;
+    int32_t reduce_mode;  // grid sums: 0 the last block to arrive, 1 every block, 2 two stages (see grid_reduce)
     int32_t blocked;      // rows: 0 interleaved over all warps, 1 contiguous range per block
     int32_t* iters;
     int32_t* sweeps;
@@ -278,7 +278,65 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
         a.partials[(size_t)bid * a.Rp * kNV + t] = s;
     }
     const int V = a.Rp * kNV;
-    if (a.two_stage) {
+    if (a.reduce_mode == 1) {
+        // every block sums all partials itself, in the same fixed order as the last
+        // block of mode 0 (so the sums are bitwise those of mode 0): no block waits
+        // for another block's sums.  The blocks arrive on a 64-bit counter that only
+        // grows; arrivals of consecutive reductions cannot interleave (a block
+        // arrives for the next one only after all have arrived for this one), so a
+        // block's own ticket tells it how many arrivals end this reduction.
+        __shared__ int s_ok1;
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long* ctr = reinterpret_cast<unsigned long long*>(a.bar + 2);
+            const unsigned long long ticket = atom_add_acqrel_u64(ctr, 1ull);
+            const unsigned long long want = (ticket / nb + 1ull) * nb;
+            int ok = 1;
+            if (ticket + 1ull != want) {
+                const unsigned long long t0 = globaltimer_ns();
+                unsigned spins = 0;
+                while (ld_acquire_u64(ctr) < want) {
+                    if (++spins > kBarrierMaxSpins || (spins & 255u) == 0u &&
+                        (globaltimer_ns() - t0 > kBarrierTimeoutNs || ld_relaxed_i32(a.status) != DEV_OK)) {
+                        atomicCAS(a.status, DEV_OK, DEV_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            s_ok1 = ok;
+        }
+        __syncthreads();
+        if (!s_ok1) return false;
+        int G = 32;
+        while (G > 1 && V * G > (int)blockDim.x) G >>= 1;
+        const int part = threadIdx.x % G;
+        for (int t0 = 0; t0 < V; t0 += blockDim.x / G) {
+            const int t = t0 + threadIdx.x / G;
+            float2 s = make_float2(0.f, 0.f);
+            if (t < V)
+                for (unsigned b0 = part; b0 < nb; b0 += 8u * G) {
+                    float2 tv[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const unsigned b = b0 + (unsigned)G * u;
+                        tv[u] = (b < nb) ? __ldcg(&a.partials[(size_t)b * V + t]) : make_float2(0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) s = dfa(s, tv[u]);
+                }
+            for (int o = G / 2; o > 0; o >>= 1)
+                s = dfa(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
+            if (part == 0 && t < V) smem[t] = s;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV; ++k) out[j][k] = smem[(r0 + j) * kNV + k].x + smem[(r0 + j) * kNV + k].y;
+    } else if (a.reduce_mode == 2) {
         if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
         // stage 2: one warp per value; lane l adds blocks l, l+32, ... and the
         // warp combines the 32 lane sums in a fixed butterfly (lane 0's order)
@@ -1155,7 +1213,7 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     for (auto* v : {&W.uh, &W.ul, &W.rh, &W.rl, &W.h0, &W.h1, &W.h2}) v->alloc(nv / 2);   // per signal
     for (auto* v : {&W.h0, &W.h1, &W.h2}) v->zero(s);
     W.sig.alloc((size_t)Rp * (1 + kMaxCompartments));
-    W.bar.alloc(2);
+    W.bar.alloc(4);   // [0], [1]: barrier / last-block arrival and release; [2..3]: 64-bit arrival counter
     W.status.alloc(1);
     W.diag.alloc(8);
     W.diag.zero(s);
@@ -1211,7 +1269,15 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     a.rtol = (float)rtol;
     a.eps_first = (float)ctx->opt_mixed_eps_first;
     a.eps_next = (float)ctx->opt_mixed_eps_next;
-    a.two_stage = ((size_t)nb * Rp * kNV > 12288) ? 1 : 0;
+    {
+        // Grid sums: two stages when one block would read too many partials; every
+        // block summing them itself when that is at most 20 loads a thread (it saves
+        // the publish / release / read-back round trips of the last-block form: 20 %
+        // on the 20^3 box, 1-2 % on the 40^3 box; slower from ~10k partial values)
+        const size_t nvals = (size_t)nb * Rp * kNV;
+        a.reduce_mode = nvals > 12288 ? 2 : (ctx->opt_mixed_reduce >= 0 ? ctx->opt_mixed_reduce
+                                                                         : (nvals <= 5120 ? 1 : 0));
+    }
     a.blocked = blocked;
     a.iters = W.iters;
     a.sweeps = W.sweeps;

@@ -175,6 +175,7 @@ struct bt_ctx {
     double opt_mixed_eps_next = 1e-2;
     int opt_mixed_extrapolate = 2;
     int opt_mixed_blocked = -1;
+    int opt_mixed_reduce = -1;   // grid sums of the mixed stepper: -1 by size, 0 last block, 1 every block
     int opt_fp64_extrapolate = 1;
 };
 
@@ -245,6 +246,16 @@ __device__ __forceinline__ unsigned atom_add_acqrel_u32(unsigned* p, unsigned v)
     unsigned old;
     asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
     return old;
+}
+__device__ __forceinline__ unsigned long long atom_add_acqrel_u64(unsigned long long* p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.add.acq_rel.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
 }
 __device__ __forceinline__ int ld_relaxed_i32(const int* p) {
     int v;

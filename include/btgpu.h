@@ -206,6 +206,8 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *   "mixed.eps_first"       inner FP32 tolerance of the first sweep (3e-6)
  *   "mixed.eps_next"        inner FP32 tolerance of later sweeps (1e-2)
  *   "mixed.blocked_rows"    rows of a block: 1 contiguous range, 0 interleaved, -1 tuned (default)
+ *   "mixed.reduce"          grid sums: 0 the last block to arrive sums and publishes, 1 every block sums
+ *                           all partials itself, -1 by size (default; same bits either way)
  *   "mixed.extrapolate"     initial guess of each step: 2 = 3u_n - 3u_{n-1} + u_{n-2} (default),
  *                           1 = 2u_n - u_{n-1}, 0 = u_n
  *   "fp64.extrapolate"      1: initial guess 2 u_n - u_{n-1} (default), 0: u_n */
