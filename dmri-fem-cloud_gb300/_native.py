@@ -33,6 +33,7 @@ EXPORTS = [
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
     "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
+    "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info",
 ]
 
 
@@ -42,6 +43,12 @@ class BtError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s (%d): %s" % (_ERRNAMES.get(code, "BT_ERR"), code, msg))
         self.code = code
+
+
+class PeriodicInfo(C.Structure):
+    _fields_ = [("active", C.c_int32), ("dir", C.c_int32 * 3), ("kappa_e", C.c_double), ("hmin", C.c_double),
+                ("n_facets", C.c_int64), ("n_rows", C.c_int64), ("n_entries", C.c_int64),
+                ("n_unmatched", C.c_int64)]
 
 
 class MeshInfo(C.Structure):
@@ -108,6 +115,9 @@ def load(path=None):
                                  C.c_int32, _D, _D, C.POINTER(Stats)]),
         "bt_solve_multi": (C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _D, _I32, C.c_double, C.c_int32,
                                      _D, _D, C.POINTER(Stats)]),
+        "bt_set_schedule_phase": (C.c_int, [_P, _D, C.c_int32, C.c_int32]),
+        "bt_set_periodic": (C.c_int, [_P, _I32]),
+        "bt_periodic_info": (C.c_int, [_P, C.POINTER(PeriodicInfo)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -214,6 +224,25 @@ class Context:
             raise ValueError("f_new and f_old must have the same shape")
         self._check(self.lib.bt_set_schedule(self.h, _dp(fn), _dp(fo), fn.shape[1], fn.shape[0],
                                              float(dt), float(theta)))
+
+    def set_schedule_phase(self, F_old):
+        """F(tp) at the explicit level of every step, [n_sequences][n_steps] (the
+        phase of the pseudo-periodic boundary term)."""
+        Fo = np.ascontiguousarray(np.atleast_2d(np.asarray(F_old, np.float64)))
+        self._check(self.lib.bt_set_schedule_phase(self.h, _dp(Fo), Fo.shape[1], Fo.shape[0]))
+
+    def set_periodic(self, periodic_dir):
+        """Weak pseudo-periodic boundaries along the axes with periodic_dir[d] = 1
+        (None or [0, 0, 0] switches them off)."""
+        d = None if periodic_dir is None else np.ascontiguousarray(np.asarray(periodic_dir, np.int32).reshape(3))
+        self._check(self.lib.bt_set_periodic(self.h, None if d is None else d.ctypes.data_as(_I32)))
+
+    def periodic_info(self):
+        pi = PeriodicInfo()
+        self._check(self.lib.bt_periodic_info(self.h, C.byref(pi)))
+        out = {k: getattr(pi, k) for k, _ in pi._fields_}
+        out["dir"] = list(pi.dir)
+        return out
 
     def solve(self, q, gdir, sequence=None, u0=None, precision=PRECISION_FP64, rtol=1e-12,
               max_iterations=2000, compartments=False):

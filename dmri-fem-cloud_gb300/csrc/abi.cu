@@ -116,6 +116,7 @@ int bt_mesh_upload(bt_ctx* ctx, const double* xyz, int64_t n_vertices, const int
         use_device(ctx);
         ctx->mat.done = false;
         ctx->coeffs = bt::Coeffs();
+        ctx->per = bt::Periodic();
         bt::free_solver64(ctx);
         bt::free_solver_mixed(ctx);
         bt::build_graph(ctx, xyz, n_vertices, tets, n_cells, cell_region, n_regions, region_compartment);
@@ -243,6 +244,50 @@ int bt_set_schedule(bt_ctx* ctx, const double* f_new, const double* f_old, int32
         S.dt = dt;
         S.theta = theta;
         S.set = true;
+        S.F_old.clear();
+        S.phase_set = false;
+    });
+}
+
+int bt_set_schedule_phase(bt_ctx* ctx, const double* F_old, int32_t n_steps, int32_t n_sequences) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        bt::Schedule& S = ctx->sched;
+        BT_REQUIRE(S.set, BT_ERR_STATE, "bt_set_schedule_phase: call bt_set_schedule first");
+        BT_REQUIRE(F_old, BT_ERR_INVALID, "bt_set_schedule_phase: NULL array");
+        BT_REQUIRE(n_steps == S.n_steps && n_sequences == S.n_seq, BT_ERR_INVALID,
+                   "bt_set_schedule_phase: sizes differ from the schedule");
+        const size_t n = (size_t)n_steps * n_sequences;
+        for (size_t i = 0; i < n; ++i)
+            BT_REQUIRE(std::isfinite(F_old[i]), BT_ERR_INVALID, "bt_set_schedule_phase: values must be finite");
+        S.F_old.assign(F_old, F_old + n);
+        S.phase_set = true;
+    });
+}
+
+int bt_set_periodic(bt_ctx* ctx, const int32_t* periodic_dir) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built, BT_ERR_STATE, "bt_set_periodic: no mesh");
+        const int32_t off[3] = {0, 0, 0};
+        use_device(ctx);
+        bt::free_solver_mixed(ctx);   // cached tuning and packed matrices do not hold the boundary term
+        bt::set_periodic(ctx, periodic_dir ? periodic_dir : off);
+    });
+}
+
+int bt_periodic_info(bt_ctx* ctx, bt_periodic_info_t* out) {
+    if (!ctx || !out) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        const bt::Periodic& P = ctx->per;
+        out->active = P.on ? 1 : 0;
+        for (int d = 0; d < 3; ++d) out->dir[d] = P.dir[d];
+        out->kappa_e = P.kappa_e;
+        out->hmin = P.hmin;
+        out->n_facets = P.n_facets;
+        out->n_rows = P.n_rows;
+        out->n_entries = P.n_entries;
+        out->n_unmatched = P.n_unmatched;
     });
 }
 

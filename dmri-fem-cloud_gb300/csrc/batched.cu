@@ -70,6 +70,8 @@ struct SolverMixed {
     DevBuf<unsigned> bar;
     DevBuf<int> status;
     DevBuf<double> fnew, fold;   // [n_seq][n_steps]
+    DevBuf<double> Fint;         // [n_seq][n_steps]: F(tp), pseudo-periodic phase
+    DevBuf<double> gvd;          // [Rp][3] gradient directions in FP64 (pseudo-periodic phase)
     DevBuf<double> qv;           // [Rp]
     DevBuf<float> gv;            // [Rp][3]
     DevBuf<int32_t> seqv;        // [Rp]
@@ -137,6 +139,14 @@ struct MixArgs {
     int32_t* sweeps;
     double* sig;  // [Rp][1+kMaxCompartments]
     float* diag;  // failure report: kind, step, sweep, iteration, worst rr2/target, RHS
+    // pseudo-periodic boundary term of the right-hand side (nullable per_ptr),
+    // evaluated in FP64 in phase S: (1 - theta) sum_e val.c e^{i q F(tp) g.(x,y,z)} u_n[col]
+    const int32_t* __restrict__ per_ptr;
+    const int32_t* __restrict__ per_col;
+    const PerVal* __restrict__ per_val;
+    const double* __restrict__ Fint;
+    const double* __restrict__ gvd;
+    double theta_d;
 };
 
 // ------------------------------------------------------------ double-float ----
@@ -557,8 +567,32 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 jg[c] = df_add(df_add(df_scale(df_norm(jx[c]), gx[0]), df_scale(df_norm(jy[c]), gy[0])),
                                df_scale(df_norm(jz[c]), gz[0]));
             // -i cs (a + i b) = cs b - i cs a
-            const DF re = df_add(df_neg(df_norm(sr[0])), df_scale(jg[1], cs[0]));
-            const DF im = df_add(df_neg(df_norm(sr[1])), df_scale(jg[0], -cs[0]));
+            DF re = df_add(df_neg(df_norm(sr[0])), df_scale(jg[1], cs[0]));
+            DF im = df_add(df_neg(df_norm(sr[1])), df_scale(jg[0], -cs[0]));
+            if (a.per_ptr) {
+                // pseudo-periodic mirror term of b, in FP64 (boundary rows only)
+                const int32_t pe0 = a.per_ptr[row], pe1 = a.per_ptr[row + 1];
+                if (pe0 < pe1) {
+                    const double ps = qd[0] * a.Fint[(size_t)sq[0] * a.sched_stride + step];
+                    const double g0 = a.gvd[r0 * 3 + 0], g1 = a.gvd[r0 * 3 + 1], g2 = a.gvd[r0 * 3 + 2];
+                    double bx = 0.0, by = 0.0;
+                    for (int32_t e = pe0; e < pe1; ++e) {
+                        const PerVal v = a.per_val[e];
+                        double sn, cs2;
+                        sincos(ps * (g0 * v.x + g1 * v.y + g2 * v.z), &sn, &cs2);
+                        const size_t ki = (size_t)a.per_col[e] * Rp4 + c4;
+                        const float2 kh = a.uh[ki], kl = a.ul[ki];
+                        const double ux = (double)kh.x + (double)kl.x, uy = (double)kh.y + (double)kl.y;
+                        bx = fma(v.c, cs2 * ux - sn * uy, bx);
+                        by = fma(v.c, sn * ux + cs2 * uy, by);
+                    }
+                    bx *= 1.0 - a.theta_d;
+                    by *= 1.0 - a.theta_d;
+                    const float bxh = (float)bx, byh = (float)by;
+                    re = df_add(re, DF{bxh, (float)(bx - (double)bxh)});
+                    im = df_add(im, DF{byh, (float)(by - (double)byh)});
+                }
+            }
             a.rh[vi] = make_float2(re.h, im.h);
             a.rl[vi] = make_float2(re.l, im.l);
         }
@@ -1074,12 +1108,14 @@ __global__ void __maxnreg__(120) k_batched_multi(const MixArgs* __restrict__ arg
 __global__ void k_pack_mixed(int64_t nnz, const double* __restrict__ M, const double* __restrict__ K,
                              const double* __restrict__ T, const double* __restrict__ R,
                              const double* __restrict__ Jx, const double* __restrict__ Jy,
-                             const double* __restrict__ Jz, double inv_k, double theta, float4* __restrict__ mA,
-                             float4* __restrict__ mL, float2* __restrict__ mS) {
+                             const double* __restrict__ Jz, double inv_k, double theta,
+                             const double* __restrict__ PB, float4* __restrict__ mA, float4* __restrict__ mL,
+                             float2* __restrict__ mS) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nnz) return;
-    const double S = K[e] + T[e] + R[e];
-    const double A = M[e] * inv_k + theta * S;
+    // S = A_re - B_re: the implicit matrix holds theta * PB, the explicit one does not
+    const double S = K[e] + T[e] + R[e] + (PB ? theta * PB[e] : 0.0);
+    const double A = M[e] * inv_k + theta * (K[e] + T[e] + R[e]) + (PB ? theta * PB[e] : 0.0);
     const double v[4] = {A, Jx[e], Jy[e], Jz[e]};
     float h[4], l[4];
 #pragma unroll
@@ -1232,6 +1268,16 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     a.mA = W.mA;
     a.mL = W.mL;
     a.mS = W.mS;
+    {
+        const Periodic& P = ctx->per;
+        a.per_ptr = P.on ? P.ptr.p : nullptr;
+        a.per_col = P.col.p;
+        a.per_val = P.val.p;
+        a.Fint = P.on ? W.Fint.p : nullptr;
+        a.gvd = W.gvd.p;
+        a.theta_d = S.theta;
+        BT_REQUIRE(!P.on || (W.Fint.p && W.gvd.p), BT_ERR_STATE, "periodic phase schedule missing");
+    }
     a.dg = W.dg;
     a.w = W.w;
     a.rcomp = W.rcomp;
@@ -1388,10 +1434,16 @@ static SolverMixed& pack_mixed(bt_ctx* ctx, const double* u0, const double** d_u
     W.iters.alloc(S.n_steps);
     W.sweeps.alloc(S.n_steps);
     k_pack_mixed<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz,
-                                                              1.0 / S.dt, S.theta, W.mA, W.mL, W.mS);
+                                                              1.0 / S.dt, S.theta,
+                                                              ctx->per.on ? ctx->per.PB.p : nullptr, W.mA, W.mL,
+                                                              W.mS);
     BT_CUDA(cudaGetLastError());
     W.fnew.upload(S.f_new.data(), S.f_new.size(), s);
     W.fold.upload(S.f_old.data(), S.f_old.size(), s);
+    if (ctx->per.on) {
+        BT_REQUIRE(S.phase_set, BT_ERR_STATE, "pseudo-periodic boundaries need bt_set_schedule_phase");
+        W.Fint.upload(S.F_old.data(), S.F_old.size(), s);
+    }
     if (u0) W.u0.upload(u0, m.n_v, s);
     *d_u0 = u0 ? W.u0.p : nullptr;
     return W;
@@ -1406,16 +1458,21 @@ static void upload_rhs(bt_ctx* ctx, SolverMixed& W, int NS, const double* q, con
     const int Rmax = kMaxRhs;
     std::vector<double> hq(Rmax);
     std::vector<float> hg(Rmax * 3);
+    std::vector<double> hgd(Rmax * 3);
     std::vector<int32_t> hs(Rmax);
     for (int r = 0; r < Rmax; ++r) {
         const int src = std::min(r / 2, NS - 1);
         hq[r] = q[src];
-        for (int k = 0; k < 3; ++k) hg[r * 3 + k] = (float)gdir[3 * src + k];
+        for (int k = 0; k < 3; ++k) {
+            hg[r * 3 + k] = (float)gdir[3 * src + k];
+            hgd[r * 3 + k] = gdir[3 * src + k];
+        }
         hs[r] = seq ? seq[src] : 0;
         BT_REQUIRE(hs[r] >= 0 && hs[r] < ctx->sched.n_seq, BT_ERR_INVALID, "sequence index out of range");
     }
     W.qv.upload(hq.data(), Rmax, s);
     W.gv.upload(hg.data(), (size_t)Rmax * 3, s);
+    W.gvd.upload(hgd.data(), (size_t)Rmax * 3, s);
     W.seqv.upload(hs.data(), Rmax, s);
 }
 

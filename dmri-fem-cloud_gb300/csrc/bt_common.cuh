@@ -143,9 +143,33 @@ struct Assembled {
 
 struct Schedule {
     std::vector<double> f_new, f_old;  // [n_seq * n_steps]
+    std::vector<double> F_old;         // integral F = int_0^t f at the explicit level (pseudo-periodic phase)
     int32_t n_steps = 0, n_seq = 0;
     double dt = 0.0, theta = 0.5;
     bool set = false;
+    bool phase_set = false;
+};
+
+// One mirror-term entry of a boundary row: coefficient and the shift of the
+// boundary vertex to its mirror point.
+struct alignas(16) PerVal {
+    double c, x, y, z;
+};
+
+// Weak pseudo-periodic boundaries (penalty form, periodic.cu): the implicit
+// matrix gains theta * PB, PB_ij = int_{exterior facets} kappa_e phi_i phi_j with
+// kappa_e the P1 interpolant of 3e-3/hmin on the periodic faces; every step's
+// right-hand side gains (1 - theta) sum_e val.c e^{i q F(tp) g.(val.x,val.y,val.z)} u_n[col]
+// over the entries of the row (PB_ij times the weight of mirror dof k in the
+// mirror point of vertex j, and the shift of vertex j).
+struct Periodic {
+    bool on = false;
+    int32_t dir[3] = {0, 0, 0};
+    double kappa_e = 0.0, hmin = 0.0;
+    int64_t n_facets = 0, n_rows = 0, n_entries = 0, n_unmatched = 0;
+    DevBuf<double> PB;            // CSR order
+    DevBuf<int32_t> ptr, col;     // [n_dofs + 1], [n_entries]
+    DevBuf<PerVal> val;           // [n_entries]
 };
 
 }  // namespace bt
@@ -160,6 +184,7 @@ struct bt_ctx {
     bt::Coeffs coeffs;
     bt::Assembled mat;
     bt::Schedule sched;
+    bt::Periodic per;
     bt::Solver64* s64 = nullptr;
     bt::SolverMixed* smx = nullptr;
     // last solve
@@ -202,6 +227,7 @@ void solve_mixed_multi(bt_ctx* const* ctxs, int32_t n_meshes, const int32_t* nsi
                        const double* gdir, const int32_t* seq, double rtol, int32_t maxit, double* sig,
                        bt_stats* st);
 void reset_tuning_mixed(bt_ctx* ctx);
+void set_periodic(bt_ctx* ctx, const int32_t* dir);
 
 void free_solvers(bt_ctx* ctx);
 double device_sum(const double* d, int64_t n, cudaStream_t s);

@@ -54,6 +54,7 @@ struct Solver64 {
     DevBuf<unsigned> bar;
     DevBuf<int> status;
     DevBuf<double> cn, co, relres, out;
+    DevBuf<double> ps;           // q F(tp) per step (pseudo-periodic phase)
     DevBuf<int32_t> iters;
     DevBuf<double> gq;           // gradient direction for the pack kernel
     DevBuf<double2> saved;       // final solutions [nsig][n_pad]
@@ -91,6 +92,15 @@ struct StepArgs {
     double rtol2;
     const double* __restrict__ rhs_vec;  // nullable: right-hand side b = rhs_vec (real) for step 0
     const double2* __restrict__ extra;   // nullable: extra[step * n_pad + i] added to b at every step
+    // pseudo-periodic boundary term (nullable per_ptr): b_i += (1 - theta) sum_e
+    // val.c exp(i ps[step] g.(val.x, val.y, val.z)) u_n[col[e]]
+    const int32_t* __restrict__ per_ptr;
+    const int32_t* __restrict__ per_col;
+    const PerVal* __restrict__ per_val;
+    const double* __restrict__ per_ps;
+    const double* __restrict__ g3;
+    double theta;
+    int64_t n_rows;
     double2* save;                       // nullable: state after step s saved to save[(s+1)/save_every - 1]
     int32_t save_every;
     int64_t n_pad;
@@ -180,6 +190,24 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 const double2 ex2 = a.extra[(int64_t)step * a.n_pad + i];
                 b.x += ex2.x;
                 b.y += ex2.y;
+            }
+            if (a.per_ptr && i < a.n_rows) {
+                const int32_t e0 = a.per_ptr[i], e1 = a.per_ptr[i + 1];
+                if (e0 < e1) {
+                    const double ps = a.per_ps[step];
+                    const double g0 = a.g3[0], g1 = a.g3[1], g2 = a.g3[2];
+                    double2 acc2 = make_double2(0.0, 0.0);
+                    for (int32_t e = e0; e < e1; ++e) {
+                        const PerVal v = a.per_val[e];
+                        double sn, cs;
+                        sincos(ps * (g0 * v.x + g1 * v.y + g2 * v.z), &sn, &cs);
+                        const double2 uk = cur[a.per_col[e]];
+                        acc2.x = fma(v.c, cs * uk.x - sn * uk.y, acc2.x);
+                        acc2.y = fma(v.c, sn * uk.x + cs * uk.y, acc2.y);
+                    }
+                    b.x = fma(1.0 - a.theta, acc2.x, b.x);
+                    b.y = fma(1.0 - a.theta, acc2.y, b.y);
+                }
             }
             // A x0 with x0 = 2 u_n - u_{n-1} (or u_n)
             const double ex = (a.extrapolate && !(a.rhs_vec && step == 0)) ? 1.0 : 0.0;
@@ -339,7 +367,8 @@ __global__ void k_pack64(int64_t sell, const int32_t* __restrict__ sl_pos, const
                          const double* __restrict__ K, const double* __restrict__ T, const double* __restrict__ R,
                          const double* __restrict__ Jx, const double* __restrict__ Jy,
                          const double* __restrict__ Jz, const double* __restrict__ g, double inv_k,
-                         double theta, double2* __restrict__ aj, double* __restrict__ bre) {
+                         double theta, const double* __restrict__ PB, double2* __restrict__ aj,
+                         double* __restrict__ bre) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= sell) return;
     const int32_t p = sl_pos[e];
@@ -350,7 +379,7 @@ __global__ void k_pack64(int64_t sell, const int32_t* __restrict__ sl_pos, const
     }
     const double mk = M[p] * inv_k;
     const double S = K[p] + T[p] + R[p];
-    aj[e] = make_double2(mk + theta * S, g[0] * Jx[p] + g[1] * Jy[p] + g[2] * Jz[p]);
+    aj[e] = make_double2(mk + theta * (PB ? S + PB[p] : S), g[0] * Jx[p] + g[1] * Jy[p] + g[2] * Jz[p]);
     bre[e] = mk - (1.0 - theta) * S;
 }
 
@@ -358,7 +387,7 @@ __global__ void k_rows64(int64_t n, int64_t n_pad, const int32_t* __restrict__ d
                          const double* __restrict__ M, const double* __restrict__ K, const double* __restrict__ T,
                          const double* __restrict__ R, const double* __restrict__ Jx,
                          const double* __restrict__ Jy, const double* __restrict__ Jz,
-                         const double* __restrict__ g, double inv_k, double theta,
+                         const double* __restrict__ g, double inv_k, double theta, const double* __restrict__ PB,
                          const double* __restrict__ wsrc, const int32_t* __restrict__ comp,
                          const int32_t* __restrict__ dof_vertex, const double* __restrict__ u0,
                          double* __restrict__ dA, double* __restrict__ dJ, double* __restrict__ w,
@@ -368,7 +397,7 @@ __global__ void k_rows64(int64_t n, int64_t n_pad, const int32_t* __restrict__ d
     if (i >= n_pad) return;
     if (i < n) {
         const int32_t p = diag_pos[i];
-        dA[i] = M[p] * inv_k + theta * (K[p] + T[p] + R[p]);
+        dA[i] = M[p] * inv_k + theta * (K[p] + T[p] + R[p] + (PB ? PB[p] : 0.0));
         dJ[i] = g[0] * Jx[p] + g[1] * Jy[p] + g[2] * Jz[p];
         w[i] = wsrc[i];
         rcomp[i] = comp[i];
@@ -430,10 +459,11 @@ static void pack_signal_fp64(bt_ctx* ctx, Solver64& W, const double* gdir, const
     cudaStream_t s = ctx->stream;
     const double inv_k = 1.0 / S.dt;
     W.gq.upload(gdir, 3, s);
+    const double* PB = ctx->per.on ? ctx->per.PB.p : nullptr;
     k_pack64<<<(unsigned)((W.sell + 255) / 256), 256, 0, s>>>(W.sell, m.sl_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy,
-                                                             A.Jz, W.gq, inv_k, S.theta, W.aj, W.bre);
+                                                             A.Jz, W.gq, inv_k, S.theta, PB, W.aj, W.bre);
     k_rows64<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(
-        m.n_dofs, W.n_pad, m.diag_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz, W.gq, inv_k, S.theta, A.w, m.dof_comp,
+        m.n_dofs, W.n_pad, m.diag_pos, A.M, A.K, A.T, A.R, A.Jx, A.Jy, A.Jz, W.gq, inv_k, S.theta, PB, A.w, m.dof_comp,
         m.dof_vertex, d_u0, W.dA, W.dJ, W.w, W.rcomp, W.u[0], W.u[2], W.u[1]);
     BT_CUDA(cudaGetLastError());
 }
@@ -464,6 +494,15 @@ static float run_steps_fp64(bt_ctx* ctx, Solver64& W, const double* d_cn, const 
     a.rtol2 = rtol * rtol;
     a.rhs_vec = rhs_vec;
     a.extra = extra;
+    const Periodic& P = ctx->per;
+    a.per_ptr = P.on ? P.ptr.p : nullptr;
+    a.per_col = P.col.p;
+    a.per_val = P.val.p;
+    a.per_ps = W.ps.p;
+    a.g3 = W.gq.p;
+    a.theta = ctx->sched.theta;
+    a.n_rows = m.n_dofs;
+    if (P.on) BT_REQUIRE(W.ps.p && W.ps.n >= (size_t)n_steps, BT_ERR_STATE, "periodic phase schedule missing");
     a.save = save;
     a.save_every = save_every > 0 ? save_every : 1;
     a.n_pad = W.n_pad;
@@ -523,7 +562,7 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
     W.saved_nsig = nsig;
     DevBuf<double> d_u0;
     if (u0) d_u0.upload(u0, m.n_v, s);
-    std::vector<double> hcn, hco, hout(kRed), hres;
+    std::vector<double> hcn, hco, hps, hout(kRed), hres;
     std::vector<int32_t> hit;
     ctx->last_iters.assign((size_t)nsig * S.n_steps, 0);
     if (st) {
@@ -542,6 +581,13 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
         schedule_row(S, seq ? seq[sg] : 0, q[sg], hcn, hco);
         W.cn.upload(hcn.data(), S.n_steps, s);
         W.co.upload(hco.data(), S.n_steps, s);
+        if (ctx->per.on) {
+            BT_REQUIRE(S.phase_set, BT_ERR_STATE, "pseudo-periodic boundaries need bt_set_schedule_phase");
+            const double* Fo = S.F_old.data() + (size_t)(seq ? seq[sg] : 0) * S.n_steps;
+            hps.resize(S.n_steps);
+            for (int k = 0; k < S.n_steps; ++k) hps[k] = q[sg] * Fo[k];
+            W.ps.upload(hps.data(), S.n_steps, s);
+        }
         pack_signal_fp64(ctx, W, gdir + 3 * sg, u0 ? d_u0.p : nullptr);
         stepper_ms_total += run_steps_fp64(ctx, W, W.cn, W.co, S.n_steps, ctx->opt_fp64_extrapolate != 0, nullptr,
                                            nullptr, 1, rtol, maxit, &hit, &hres, hout.data());
@@ -726,6 +772,8 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
                "bt_adjoint: gradients are defined for per-region isotropic D (clear the per-cell tensor)");
     BT_REQUIRE(!ctx->coeffs.has_cell_T2, BT_ERR_STATE,
                "bt_adjoint: gradients are defined for per-region 1/T2 (clear the per-cell T2)");
+    BT_REQUIRE(!ctx->per.on, BT_ERR_STATE,
+               "bt_adjoint: not defined with pseudo-periodic boundaries (the mirror term is not transposed)");
     if (!ctx->s64) ctx->s64 = new Solver64();
     Solver64& W = *ctx->s64;
     prepare_fp64(ctx, W);
@@ -909,6 +957,7 @@ void tangent_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
     cudaStream_t s = ctx->stream;
     BT_REQUIRE(!ctx->coeffs.has_cell_D && !ctx->coeffs.has_cell_T2, BT_ERR_STATE,
                "bt_tangent: derivatives are defined for per-region coefficients (clear per-cell D / T2)");
+    BT_REQUIRE(!ctx->per.on, BT_ERR_STATE, "bt_tangent: not defined with pseudo-periodic boundaries");
     const int nr = m.n_regions;
     BT_REQUIRE(kind >= 0 && kind <= 2 && ri >= 0 && ri < nr && (kind != 2 || (rj >= 0 && rj < nr && rj != ri)),
                BT_ERR_INVALID, "bt_tangent: bad parameter");

@@ -224,6 +224,14 @@ def profile_samples(profile, k, loop="solve"):
     return (np.array([profile.f(t) for t in tn]), np.array([profile.f(t) for t in to]))
 
 
+def phase_samples(profile, k, loop="solve"):
+    """F(tp) = int_0^tp f at the explicit level of every step: the phase of the
+    pseudo-periodic boundary term (``itime_profile(tp)`` handed to
+    ``WeakPseudoPeriodic.set_values``, ``DmriFemLib.py:73, 117, 901-905``)."""
+    _, to = schedule(profile.T, k, loop)
+    return np.array([profile.F(t) for t in to])
+
+
 def b_to_q(bvalue, int4gb):
     """``convert_b2q`` (``DmriFemLib.py:840-842``)."""
     return math.sqrt(bvalue) / math.sqrt(int4gb)

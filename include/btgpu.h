@@ -63,6 +63,17 @@ typedef struct bt_mesh_info_t {
     double volume;               /* sum of cell volumes                         */
 } bt_mesh_info_t;
 
+typedef struct bt_periodic_info_t {
+    int32_t active;              /* 1 when a periodic direction is set          */
+    int32_t dir[3];              /* PeriodicDir                                 */
+    double kappa_e;              /* penalty 3e-3 / hmin                         */
+    double hmin;                 /* smallest cell diameter                      */
+    int64_t n_facets;            /* exterior facets with a nonzero penalty      */
+    int64_t n_rows;              /* dofs with a mirror term                     */
+    int64_t n_entries;           /* mirror-term entries                         */
+    int64_t n_unmatched;         /* mirror points outside every face triangle   */
+} bt_periodic_info_t;
+
 typedef struct bt_stats_t {
     int32_t steps;               /* time steps per signal                       */
     int32_t max_iterations;      /* largest inner iteration count of any step   */
@@ -135,6 +146,27 @@ int bt_assemble(bt_ctx* ctx);
  * dt = mri_simu.k, theta = mri_simu.theta. */
 int bt_set_schedule(bt_ctx* ctx, const double* f_new, const double* f_old,
                     int32_t n_steps, int32_t n_sequences, double dt, double theta);
+
+/* Phase schedule of the pseudo-periodic boundary term: F_old[n_sequences*n_steps]
+ * = F(tp) = int_0^tp f at the explicit level of each step (the itime_profile
+ * value the reference passes to WeakPseudoPeriodic.set_values, DmriFemLib.py:
+ * 73, 117, 901-905).  Sizes must equal the schedule's; bt_set_schedule clears
+ * it.  Needed only when periodic directions are set. */
+int bt_set_schedule_phase(bt_ctx* ctx, const double* F_old, int32_t n_steps, int32_t n_sequences);
+
+/* Weak pseudo-periodic boundary conditions: periodic_dir[3] = mydomain.PeriodicDir
+ * (0/1 per axis; all 0 or NULL switches them off), the reference's default
+ * form when IsDomainPeriodic is False (ThetaMethodF/L_wBC1c/2c,
+ * DmriFemLib.py:58-145, WeakPseudoPeriodic_1c/2c :256-323, :386-451,
+ * WeakPseudoPeridicMarker :598-610).  The implicit matrix gains
+ * theta int kappa_e u v ds, every step's right-hand side gains
+ * (1-theta) int kappa_e ubc v ds with ubc = u_n at the mirror point on the
+ * opposite face times exp(i q F(tp) g.shift).  The box is the mesh's bounding
+ * box; the mesh need not be periodic.  Call after bt_mesh_upload (a new mesh
+ * clears it); the strong form (IsDomainPeriodic, a constrained periodic space)
+ * is not provided.  bt_adjoint and bt_tangent reject a periodic context. */
+int bt_set_periodic(bt_ctx* ctx, const int32_t* periodic_dir);
+int bt_periodic_info(bt_ctx* ctx, bt_periodic_info_t* out);
 
 /* Integrate n_signals Bloch-Torrey problems and return their signals.
  *   q[n_signals]            mri_para.qvalue

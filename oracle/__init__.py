@@ -20,6 +20,8 @@ run.  The restatement follows the reference's forms line by line:
   ``while t < T + k``), ``PostProcessing`` signal (``DmriFemLib.py:917-931``).
 * ``sequence.py``-- ``MRI_parameters`` (``DmriFemLib.py:800-858``): f(t), the
   b -> q conversion through int_0^T (int_0^s f)^2.
+* ``periodic.py``-- the weak pseudo-periodic boundary term (``DmriFemLib.py:
+  58-145, 256-323, 386-451, 596-610``): boundary penalty matrix and mirror map.
 * ``mesh.py``    -- DOLFIN ``BoxMesh`` (6 tets per cube around the
   (0,0,0)->(1,1,1) diagonal), used by the reference's ``ConvergenceTest``.
 
@@ -45,3 +47,4 @@ from .forms import (  # noqa: F401
 from .loop import (  # noqa: F401
     solve_duplicated, solve_two_field, OracleResult,
 )
+from .periodic import weak_periodic  # noqa: F401

@@ -61,12 +61,14 @@ def _jacobi_bicgstab(A, b, rtol, atol, maxiter):
 
 
 def solve_duplicated(sysd, seq, q, gdir, k, theta=0.5, loop="solve", u0=None,
-                     solver="lu", rtol=1e-9, atol=1e-10, max_steps=None):
+                     solver="lu", rtol=1e-9, atol=1e-10, max_steps=None, periodic=None):
     """Time loop on the complex duplicated-node system of ``forms.duplicated_system``.
 
     ``q`` is ``mri_para.qvalue``; ``gdir`` is normalised as in
     ``set_gradient_dir`` (``DmriFemLib.py:809-824``).  ``max_steps`` truncates
-    the loop (bounded CPU-timing samples only).
+    the loop (bounded CPU-timing samples only).  ``periodic`` is the output of
+    ``periodic.weak_periodic``: the implicit matrix gains theta B and every
+    right-hand side (1 - theta) B ubc(u_n, F(tp)) (``DmriFemLib.py:58-145``).
     """
     g = np.asarray(gdir, dtype=np.float64)
     g = g / np.linalg.norm(g)
@@ -83,12 +85,20 @@ def solve_duplicated(sysd, seq, q, gdir, k, theta=0.5, loop="solve", u0=None,
     S0 = float(np.dot(sysd["vertex_weight"], ic))
     Abase = (Mk + theta * S).astype(np.complex128).tocsc()
     Bbase = (Mk - (1.0 - theta) * S).astype(np.complex128).tocsr()
+    if periodic is not None:
+        from .periodic import ubc
+        Abase = (Abase + theta * periodic["B"].astype(np.complex128)).tocsc()
+        Bper = periodic["B"].astype(np.complex128).tocsr()
+        _, t_old = reference_schedule(seq.T, k, loop)
+        F_old = np.array([seq.F(t) for t in t_old])[:len(f_old)]
     Jc = Jg.astype(np.complex128)
     cache = {}
     iters = []
     t0 = time.perf_counter()
-    for fn, fo in zip(f_new, f_old):
+    for step, (fn, fo) in enumerate(zip(f_new, f_old)):
         rhs = Bbase @ u - 1j * ((1.0 - theta) * q * fo) * (Jc @ u)
+        if periodic is not None:
+            rhs = rhs + (1.0 - theta) * (Bper @ ubc(periodic, u, q, g, F_old[step]))
         A = (Abase + 1j * (theta * q * fn) * Jc.tocsc())
         if solver == "lu":
             lu = cache.get(fn)

@@ -80,13 +80,27 @@ def test_sympy_profile_matches(pkg):
     assert para.time_profile(10600.0) == 0.0 and para.time_profile(200.0) == 1.0
 
 
-def test_periodic_rejected(pkg):
+def test_strong_periodic_rejected(pkg):
+    """The weak pseudo-periodic form is accepted; the strong one (a constrained
+    periodic space, IsDomainPeriodic = True) is not provided."""
     mesh = pkg.Mesh(*pkg.meshgen.kuhn_box(-1, 1, 2))
     para = pkg.MRI_parameters()
     dom = pkg.MyDomain(mesh, para)
     dom.PeriodicDir = [1, 0, 0]
+    dom.Apply()
+    dom.IsDomainPeriodic = True
     with pytest.raises(NotImplementedError):
         dom.Apply()
+
+
+def test_phase_samples(pkg):
+    """F(tp) on the explicit level: F(0) at the first step, then F((n-1) k)."""
+    p = pkg.sequences.pgse(1000.0, 3000.0)
+    F = pkg.sequences.phase_samples(p, 200.0)
+    fn, fo = pkg.sequences.profile_samples(p, 200.0)
+    assert len(F) == len(fo) and F[0] == 0.0
+    assert abs(F[1] - p.F(0.0)) < 1e-15 and abs(F[2] - p.F(200.0)) < 1e-12
+    assert abs(F[-1] - p.F((len(F) - 2) * 200.0)) < 1e-9
 
 
 def test_domain_regions(pkg):
