@@ -33,7 +33,7 @@ EXPORTS = [
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
     "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
-    "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info",
+    "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info", "bt_adjoint_batch",
 ]
 
 
@@ -118,6 +118,8 @@ def load(path=None):
         "bt_set_schedule_phase": (C.c_int, [_P, _D, C.c_int32, C.c_int32]),
         "bt_set_periodic": (C.c_int, [_P, _I32]),
         "bt_periodic_info": (C.c_int, [_P, C.POINTER(PeriodicInfo)]),
+        "bt_adjoint_batch": (C.c_int, [_P, C.c_int32, _D, _D, _I32, C.c_double, C.c_int32, C.c_int32,
+                                       _D, _D, _D, _D, C.POINTER(Stats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -278,6 +280,22 @@ class Context:
                                         C.byref(st)))
         return {"signal": float(sig[0]), "dD": dD, "dinvT2": dT, "dkappa": dK.reshape(nr, nr),
                 "stats": st.as_dict()}
+
+    def adjoint_batch(self, q, gdir, sequence=None, rtol=1e-9, max_iterations=20000, stride=0):
+        """The discrete adjoint of many signals at once in mixed precision:
+        signal[n], dD[n, nr], dinvT2[n, nr], dkappa[n, nr, nr] (unnormalised)."""
+        q = np.ascontiguousarray(np.atleast_1d(np.asarray(q, np.float64)))
+        n = len(q)
+        g = np.ascontiguousarray(np.asarray(gdir, np.float64).reshape(n, 3))
+        seq = None if sequence is None else np.ascontiguousarray(np.asarray(sequence, np.int32).reshape(n))
+        nr = self.n_regions
+        sig = np.zeros(n)
+        dD, dT, dK = np.zeros(n * nr), np.zeros(n * nr), np.zeros(n * nr * nr)
+        st = Stats()
+        self._check(self.lib.bt_adjoint_batch(self.h, n, _dp(q), _dp(g), _ip(seq), float(rtol), int(max_iterations),
+                                              int(stride), _dp(sig), _dp(dD), _dp(dT), _dp(dK), C.byref(st)))
+        return {"signal": sig, "dD": dD.reshape(n, nr), "dinvT2": dT.reshape(n, nr),
+                "dkappa": dK.reshape(n, nr, nr), "stats": st.as_dict()}
 
     def tangent(self, q, gdir, param, i, j=0, sequence=0, u0=None, rtol=1e-13, max_iterations=5000):
         """Signal and d(signal)/d(param) by a tangent-linear FP64 run; param is

@@ -422,6 +422,27 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
     });
 }
 
+int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir, const int32_t* sequence,
+                     double rtol, int32_t max_iterations, int32_t checkpoint_stride, double* signal_out,
+                     double* dS_dD, double* dS_dinvT2, double* dS_dkappa, bt_stats* stats) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint_batch: mesh not assembled");
+        BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_adjoint_batch: no schedule");
+        BT_REQUIRE(n_signals >= 1 && q && gdir && signal_out, BT_ERR_INVALID, "bt_adjoint_batch: bad arguments");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_adjoint_batch: rtol must be > 0 and max_iterations >= 1");
+        for (int32_t i = 0; i < n_signals; ++i)
+            BT_REQUIRE(std::isfinite(q[i]) && std::isfinite(gdir[3 * i]) && std::isfinite(gdir[3 * i + 1]) &&
+                           std::isfinite(gdir[3 * i + 2]),
+                       BT_ERR_INVALID, "bt_adjoint_batch: q and gdir must be finite");
+        use_device(ctx);
+        ctx->last_precision = -1;
+        bt::adjoint_mixed(ctx, n_signals, q, gdir, sequence, rtol, max_iterations, checkpoint_stride, signal_out,
+                          dS_dD, dS_dinvT2, dS_dkappa, stats);
+    });
+}
+
 int bt_set_option(bt_ctx* ctx, const char* key, double value) {
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {

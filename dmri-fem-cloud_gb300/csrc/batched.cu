@@ -147,6 +147,13 @@ struct MixArgs {
     const double* __restrict__ Fint;
     const double* __restrict__ gvd;
     double theta_d;
+    // discrete adjoint (adjoint_mixed): the first step's right-hand side is the
+    // signal weight w (from a zero state), and the state after every save_every-th
+    // step is copied to save_h / save_l [(step + 1) / save_every - 1][n][Rp/2]
+    int32_t rhs_w;
+    int32_t save_every;
+    float2* save_h;
+    float2* save_l;
 };
 
 // ------------------------------------------------------------ double-float ----
@@ -593,6 +600,11 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                     im = df_add(im, DF{byh, (float)(by - (double)byh)});
                 }
             }
+            if (a.rhs_w && step == 0) {   // b = w from the zero state: r = w
+                const double wv = a.w[row];
+                const float wh = (float)wv;
+                re = df_add(re, DF{wh, (float)(wv - (double)wh)});
+            }
             a.rh[vi] = make_float2(re.h, im.h);
             a.rl[vi] = make_float2(re.l, im.l);
         }
@@ -687,7 +699,8 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             kadd(red[1][0], im.h * z1.x);
             kadd(red[1][1], im.h * z1.y);
             kadd(red[1][2], im.h * im.h);
-            const float bn = wr * wr * (uhr.x * uhr.x + uhr.y * uhr.y);
+            const float bn = (a.rhs_w && step == 0) ? (float)(a.w[row] * a.w[row])
+                                                    : wr * wr * (uhr.x * uhr.x + uhr.y * uhr.y);
             kadd(red[0][3], bn);
             kadd(red[1][3], bn);
         }
@@ -1030,6 +1043,17 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             a.sweeps[step] = sweep;
         }
         if (failed) return;
+        if (a.save_h && (step + 1) % a.save_every == 0) {
+            // every lane copies its own (row, signal) entries, which it wrote itself in phase U
+            const size_t off = (size_t)((step + 1) / a.save_every - 1) * a.n * Rp4;
+            for (int g = g0; g < gend; g += gstride) {
+                const int row = g * G + slot;
+                if (row >= a.n) continue;
+                const size_t vi = (size_t)row * Rp4 + c4;
+                a.save_h[off + vi] = a.uh[vi];
+                a.save_l[off + vi] = a.ul[vi];
+            }
+        }
     }
 #undef BT_REDUCE
     // ---- signal: FP64 sums of w Re(u) per RHS and compartment (lanes own their RHS)
@@ -1276,6 +1300,10 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
         a.Fint = P.on ? W.Fint.p : nullptr;
         a.gvd = W.gvd.p;
         a.theta_d = S.theta;
+        a.rhs_w = 0;
+        a.save_every = 1;
+        a.save_h = nullptr;
+        a.save_l = nullptr;
         BT_REQUIRE(!P.on || (W.Fint.p && W.gvd.p), BT_ERR_STATE, "periodic phase schedule missing");
     }
     a.dg = W.dg;
@@ -1363,8 +1391,24 @@ static void check_batch(SolverMixed& W, int lpr, int nb, cudaStream_t s) {
 
 // Launch one batch (R <= 512 slots) on one mesh with the given geometry.
 // Returns the device time of the stepper kernel (ms).
+// Launch options of the discrete adjoint: the initial per-signal state (copied
+// over the one prepare_batch sets, or zero), per-step saves, the w right-hand
+// side of the first step, and a schedule other than the context's (pointers
+// already offset to the first step, rows of sched_stride steps).
+struct MixExtra {
+    const float2* init_h = nullptr;
+    const float2* init_l = nullptr;
+    bool zero_init = false;
+    float2* save_h = nullptr;
+    float2* save_l = nullptr;
+    int save_every = 1;
+    int rhs_w = 0;
+    const double* fnew = nullptr;
+    const double* fold = nullptr;
+};
+
 static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int blocked, int n_steps,
-                          double rtol, int maxit, const double* d_u0) {
+                          double rtol, int maxit, const double* d_u0, const MixExtra* ex = nullptr) {
     cudaStream_t s = ctx->stream;
     KFn fn = kernel_for(lpr);
     int occ = 0;
@@ -1373,6 +1417,24 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     const int per_sm = std::max(1, std::min(occ, per_sm_blocks));
     const int nb = std::max(1, std::min(per_sm * ctx->num_sms, blocks_needed(ctx, R, lpr)));
     MixArgs a = prepare_batch(ctx, W, R, lpr, nb, blocked, n_steps, rtol, maxit, d_u0);
+    if (ex) {
+        const size_t vsz = (size_t)ctx->mesh.n_dofs * (a.Rp / 2);
+        if (ex->zero_init) {
+            W.uh.zero(s);
+            W.ul.zero(s);
+        } else if (ex->init_h) {
+            BT_CUDA(cudaMemcpyAsync(W.uh.p, ex->init_h, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+            BT_CUDA(cudaMemcpyAsync(W.ul.p, ex->init_l, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+        }
+        a.save_h = ex->save_h;
+        a.save_l = ex->save_l;
+        a.save_every = std::max(1, ex->save_every);
+        a.rhs_w = ex->rhs_w;
+        if (ex->fnew) {
+            a.fnew = ex->fnew;
+            a.fold = ex->fold;
+        }
+    }
     void* args[] = {&a};
     BT_CUDA(cudaEventRecord(ctx->ev1, s));
     BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(nb), dim3(kThreadsB), args, 0, s));
@@ -1825,6 +1887,351 @@ void reset_tuning_mixed(bt_ctx* ctx) {
 void free_solver_mixed(bt_ctx* ctx) {
     delete ctx->smx;
     ctx->smx = nullptr;
+}
+
+// ------------------------------------------------------- batched discrete adjoint
+// The FP64 adjoint of stepper64.cu (adjoint_fp64) for a whole batch of signals in
+// mixed precision: with A_n u_{n+1} = B_n u_n and Sig = w^T Re(u_N),
+//     A_{N-1} lambda_N = w,   A_{n-1} lambda_n = B_n lambda_{n+1}  (A, B complex symmetric),
+//     dSig/dxi = -Re sum_n lambda_{n+1}^T (dS/dxi) (theta u_{n+1} + (1 - theta) u_n).
+// A backward step is a forward step of the batched stepper with the schedule
+// pair (f_new[n-1], f_old[n]), so the same kernel runs both directions; forward
+// states are recomputed segment by segment from checkpoints every stride steps.
+namespace {
+
+// per-cell gradient products: upper triangle of grad(phi_r).grad(phi_c) * vol, and vol
+__global__ void k_cell_kmat(int64_t n_t, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                            double* __restrict__ kmat) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_t) return;
+    double X[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) X[k][c] = xyz[(int64_t)tets[t * 4 + k] * 3 + c];
+    double E[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) E[r][c] = X[r + 1][c] - X[0][c];
+    const double c00 = E[1][1] * E[2][2] - E[1][2] * E[2][1];
+    const double c01 = E[1][2] * E[2][0] - E[1][0] * E[2][2];
+    const double c02 = E[1][0] * E[2][1] - E[1][1] * E[2][0];
+    const double det = E[0][0] * c00 + E[0][1] * c01 + E[0][2] * c02;
+    const double id = 1.0 / det;
+    double G[4][3];
+    G[1][0] = c00 * id; G[1][1] = c01 * id; G[1][2] = c02 * id;
+    G[2][0] = (E[0][2] * E[2][1] - E[0][1] * E[2][2]) * id;
+    G[2][1] = (E[0][0] * E[2][2] - E[0][2] * E[2][0]) * id;
+    G[2][2] = (E[0][1] * E[2][0] - E[0][0] * E[2][1]) * id;
+    G[3][0] = (E[0][1] * E[1][2] - E[0][2] * E[1][1]) * id;
+    G[3][1] = (E[0][2] * E[1][0] - E[0][0] * E[1][2]) * id;
+    G[3][2] = (E[0][0] * E[1][1] - E[0][1] * E[1][0]) * id;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) G[0][c] = -(G[1][c] + G[2][c] + G[3][c]);
+    const double vol = fabs(det) / 6.0;
+    int k = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = r; c < 4; ++c)
+            kmat[t * 11 + k++] = vol * (G[r][0] * G[c][0] + G[r][1] * G[c][1] + G[r][2] * G[c][2]);
+    kmat[t * 11 + 10] = vol;
+}
+
+__device__ __forceinline__ double2 state_at(const float2* __restrict__ h, const float2* __restrict__ l, size_t i) {
+    const float2 a = h[i], b = l[i];
+    return make_double2((double)a.x + (double)b.x, (double)a.y + (double)b.y);
+}
+
+// accD[t][s] -= Re(L^T K V), accT[t][s] -= Re(L^T M V) of cell t, signal s (unit coefficients)
+__global__ void k_adjb_cells(int64_t n_t, int NS, int ns, const double* __restrict__ kmat,
+                             const int32_t* __restrict__ tets, const int32_t* __restrict__ comp,
+                             const int32_t* __restrict__ dof_of, int nc, const float2* __restrict__ lh,
+                             const float2* __restrict__ ll, const float2* __restrict__ u0h,
+                             const float2* __restrict__ u0l, const float2* __restrict__ u1h,
+                             const float2* __restrict__ u1l, double theta, double* __restrict__ accD,
+                             double* __restrict__ accT) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n_t * NS) return;
+    const int64_t t = idx / NS;
+    const int sg = (int)(idx % NS);
+    const int f = comp[t];
+    double2 L[4], V[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t i = (size_t)dof_of[(int64_t)tets[t * 4 + k] * nc + f] * ns + sg;
+        L[k] = state_at(lh, ll, i);
+        const double2 a0 = state_at(u0h, u0l, i), a1 = state_at(u1h, u1l, i);
+        V[k] = make_double2(theta * a1.x + (1.0 - theta) * a0.x, theta * a1.y + (1.0 - theta) * a0.y);
+    }
+    const double* km = kmat + t * 11;
+    const double vol = km[10];
+    double sK = 0.0, sM = 0.0;
+    int k = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = r; c < 4; ++c) {
+            // symmetric: (r, c) and (c, r) together
+            const double re = L[r].x * V[c].x - L[r].y * V[c].y +
+                              (r == c ? 0.0 : L[c].x * V[r].x - L[c].y * V[r].y);
+            sK += km[k++] * re;
+            sM += (r == c ? vol / 10.0 : vol / 20.0) * re;
+        }
+    accD[idx] -= sK;
+    accT[idx] -= sM;
+}
+
+// accK[i][s] -= Re([L]^T B [V]) of interface facet i (facet mass, jumps across the duplicated dofs)
+__global__ void k_adjb_facets(int64_t n_if, int NS, int ns, const int32_t* __restrict__ fcell,
+                              const int32_t* __restrict__ fface, const double* __restrict__ xyz,
+                              const int32_t* __restrict__ tets, const int32_t* __restrict__ nbr,
+                              const int32_t* __restrict__ comp, const int32_t* __restrict__ dof_of, int nc,
+                              const float2* __restrict__ lh, const float2* __restrict__ ll,
+                              const float2* __restrict__ u0h, const float2* __restrict__ u0l,
+                              const float2* __restrict__ u1h, const float2* __restrict__ u1l, double theta,
+                              double* __restrict__ accK) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n_if * NS) return;
+    const int64_t i = idx / NS;
+    const int sg = (int)(idx % NS);
+    const int32_t t = fcell[i];
+    const int fa = fface[i];
+    const int32_t nb = nbr[(int64_t)t * 4 + fa];
+    const int f = comp[t], g = comp[nb];
+    int32_t fv[3];
+    int m = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k != fa) fv[m++] = tets[(int64_t)t * 4 + k];
+    double e1[3], e2[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        e1[c] = xyz[(int64_t)fv[1] * 3 + c] - xyz[(int64_t)fv[0] * 3 + c];
+        e2[c] = xyz[(int64_t)fv[2] * 3 + c] - xyz[(int64_t)fv[0] * 3 + c];
+    }
+    const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                 cz = e1[0] * e2[1] - e1[1] * e2[0];
+    const double area = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+    double2 Lj[3], Vj[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const size_t da = (size_t)dof_of[(int64_t)fv[k] * nc + f] * ns + sg;
+        const size_t db = (size_t)dof_of[(int64_t)fv[k] * nc + g] * ns + sg;
+        const double2 la = state_at(lh, ll, da), lb = state_at(lh, ll, db);
+        const double2 ua0 = state_at(u0h, u0l, da), ua1 = state_at(u1h, u1l, da);
+        const double2 ub0 = state_at(u0h, u0l, db), ub1 = state_at(u1h, u1l, db);
+        Lj[k] = make_double2(la.x - lb.x, la.y - lb.y);
+        Vj[k] = make_double2(theta * (ua1.x - ub1.x) + (1.0 - theta) * (ua0.x - ub0.x),
+                             theta * (ua1.y - ub1.y) + (1.0 - theta) * (ua0.y - ub0.y));
+    }
+    double sK = 0.0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            sK += (r == c ? area / 6.0 : area / 12.0) * (Lj[r].x * Vj[c].x - Lj[r].y * Vj[c].y);
+    accK[idx] -= sK;
+}
+
+// out[s][k] = sum over items i with key[i] == k of acc[i][s], in a fixed order
+// (grid: NS x n_keys blocks of 256 threads)
+__global__ void k_adjb_reduce(int64_t n_items, int NS, const int32_t* __restrict__ key, int n_keys,
+                              const double* __restrict__ acc, double* __restrict__ out) {
+    __shared__ double sm[256];
+    const int sg = blockIdx.x, kk = blockIdx.y;
+    double v = 0.0;
+    for (int64_t i = threadIdx.x; i < n_items; i += blockDim.x)
+        if (key[i] == kk) v += acc[i * NS + sg];
+    sm[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(size_t)sg * n_keys + kk] = sm[0];
+}
+
+}  // namespace
+
+void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
+                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
+                   bt_stats* st) {
+    Mesh& m = ctx->mesh;
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    BT_REQUIRE(!ctx->coeffs.has_cell_D && !ctx->coeffs.has_cell_T2, BT_ERR_STATE,
+               "bt_adjoint_batch: gradients are defined for per-region coefficients (clear per-cell D / T2)");
+    BT_REQUIRE(!ctx->per.on, BT_ERR_STATE, "bt_adjoint_batch: not defined with pseudo-periodic boundaries");
+    const double* d_u0 = nullptr;
+    SolverMixed& W = pack_mixed(ctx, nullptr, &d_u0);
+    const int N = S.n_steps, nr = m.n_regions;
+    const double th = S.theta;
+    if (stride <= 0) stride = (int)std::ceil(std::sqrt((double)N));
+    stride = std::max(1, std::min(stride, N));
+    const int nck = (N + stride - 1) / stride;
+    // adjoint schedule: backward step j builds lambda_{N-j} with f_new[N-1-j] and f_old[N-j]
+    std::vector<double> afn((size_t)S.n_seq * N), afo((size_t)S.n_seq * N, 0.0);
+    for (int r = 0; r < S.n_seq; ++r)
+        for (int j = 0; j < N; ++j) {
+            afn[(size_t)r * N + j] = S.f_new[(size_t)r * N + N - 1 - j];
+            if (j >= 1) afo[(size_t)r * N + j] = S.f_old[(size_t)r * N + N - j];
+        }
+    DevBuf<double> d_afn, d_afo, kmat, accD, accT, accK, red;
+    d_afn.upload(afn.data(), afn.size(), s);
+    d_afo.upload(afo.data(), afo.size(), s);
+    kmat.alloc((size_t)m.n_t * 11);
+    k_cell_kmat<<<(unsigned)((m.n_t + 127) / 128), 128, 0, s>>>(m.n_t, m.xyz, m.tets, kmat);
+    BT_CUDA(cudaGetLastError());
+    // interface facet -> region pair (r1 <= r2) index r1 * nr + r2
+    std::vector<int32_t> hreg(m.n_t), hpair(std::max<int64_t>(1, m.n_iface), 0);
+    m.region.download(hreg.data(), m.n_t, s);
+    if (m.n_iface > 0) {
+        std::vector<int32_t> hfc(m.n_iface), hff(m.n_iface), hnb((size_t)m.n_t * 4);
+        m.iface_cell.download(hfc.data(), m.n_iface, s);
+        m.iface_face.download(hff.data(), m.n_iface, s);
+        m.nbr.download(hnb.data(), hnb.size(), s);
+        BT_CUDA(cudaStreamSynchronize(s));
+        for (int64_t i = 0; i < m.n_iface; ++i) {
+            const int32_t t = hfc[i], nb = hnb[(size_t)t * 4 + hff[i]];
+            hpair[i] = std::min(hreg[t], hreg[nb]) * nr + std::max(hreg[t], hreg[nb]);
+        }
+    }
+    DevBuf<int32_t> pair;
+    pair.upload(hpair.data(), hpair.size(), s);
+    reset_stats(st, N, rtol);
+    ctx->last_iters.assign((size_t)nsig * N, 0);   // collect_batch records the forward sweep's counts
+    W.saved.clear();
+    W.saved_nsig = 0;
+    float ms = 0.0f;
+    int64_t launches = 1;
+    BT_CUDA(cudaEventRecord(ctx->ev0, s));
+    std::vector<double> hD, hT, hK;
+    for (int32_t b0 = 0; b0 < nsig; b0 += kMaxRhs / 2) {
+        const int NS = std::min<int32_t>(kMaxRhs / 2, nsig - b0);
+        const int R = 2 * NS;
+        upload_rhs(ctx, W, NS, q + b0, gdir + 3 * b0, seq ? seq + b0 : nullptr);
+        const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, d_u0);
+        const int Rp = padded_rhs(R, geo.lpr), ns = Rp / 2;
+        const size_t vsz = (size_t)m.n_dofs * ns;
+        DevBuf<float2> ckh, ckl, sgh, sgl, bkh, bkl, lch, lcl;
+        ckh.alloc((nck + 1) * vsz); ckl.alloc((nck + 1) * vsz);
+        sgh.alloc((stride + 1) * vsz); sgl.alloc((stride + 1) * vsz);
+        bkh.alloc(stride * vsz); bkl.alloc(stride * vsz);
+        lch.alloc(vsz); lcl.alloc(vsz);
+        accD.alloc((size_t)m.n_t * NS); accD.zero(s);
+        accT.alloc((size_t)m.n_t * NS); accT.zero(s);
+        accK.alloc((size_t)std::max<int64_t>(1, m.n_iface) * NS); accK.zero(s);
+        auto run = [&](int n_steps, const MixExtra& ex) {
+            ms += launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, n_steps, rtol, maxit, d_u0, &ex);
+            ++launches;
+        };
+        // checkpoint 0: the initial state (u0 = 1), in the batch's layout
+        k_rows_mixed<<<(unsigned)((m.n_dofs + 255) / 256), 256, 0, s>>>(m.n_dofs, Rp, R, m.diag_pos, W.mA,
+                                                                        ctx->mat.w, m.dof_comp, m.dof_vertex,
+                                                                        nullptr, W.dg, W.w, W.rcomp, ckh.p, ckl.p);
+        BT_CUDA(cudaGetLastError());
+        {   // forward: u_{j stride} into checkpoint j, and the signals
+            MixExtra ex;
+            ex.save_h = ckh.p + vsz;
+            ex.save_l = ckl.p + vsz;
+            ex.save_every = stride;
+            run(N, ex);
+            collect_batch(ctx, W, b0, NS, false, sig + b0, nullptr, nullptr);
+        }
+        {   // lambda_N = A_{N-1}^{-1} w from the zero state
+            MixExtra ex;
+            ex.zero_init = true;
+            ex.rhs_w = 1;
+            ex.fnew = d_afn.p;
+            ex.fold = d_afo.p;
+            run(1, ex);
+            BT_CUDA(cudaMemcpyAsync(lch.p, W.uh.p, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+            BT_CUDA(cudaMemcpyAsync(lcl.p, W.ul.p, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+        }
+        const unsigned cb = (unsigned)((m.n_t * NS + 255) / 256), fb = (unsigned)((m.n_iface * NS + 255) / 256);
+        for (int sgm = nck - 1; sgm >= 0; --sgm) {
+            const int a0 = sgm * stride, e0 = std::min(a0 + stride, N), len = e0 - a0;
+            // u_{a0..e0}: seg[k] = u_{a0+k}
+            BT_CUDA(cudaMemcpyAsync(sgh.p, ckh.p + (size_t)sgm * vsz, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+            BT_CUDA(cudaMemcpyAsync(sgl.p, ckl.p + (size_t)sgm * vsz, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+            {
+                MixExtra ex;
+                ex.init_h = sgh.p;
+                ex.init_l = sgl.p;
+                ex.save_h = sgh.p + vsz;
+                ex.save_l = sgl.p + vsz;
+                ex.fnew = W.fnew.p + a0;
+                ex.fold = W.fold.p + a0;
+                run(len, ex);
+            }
+            // lambda_{e0-1} ... lambda_{a0} (lambda_0 is not needed): bk[k] = lambda_{e0-1-k}
+            const int nb_steps = (a0 == 0) ? len - 1 : len;
+            if (nb_steps > 0) {
+                MixExtra ex;
+                ex.init_h = lch.p;
+                ex.init_l = lcl.p;
+                ex.save_h = bkh.p;
+                ex.save_l = bkl.p;
+                ex.fnew = d_afn.p + (N - e0 + 1);
+                ex.fold = d_afo.p + (N - e0 + 1);
+                run(nb_steps, ex);
+            }
+            for (int n = e0 - 1; n >= a0; --n) {
+                const float2* Lh = (n + 1 == e0) ? lch.p : bkh.p + (size_t)(e0 - 2 - n) * vsz;
+                const float2* Ll = (n + 1 == e0) ? lcl.p : bkl.p + (size_t)(e0 - 2 - n) * vsz;
+                const size_t o0 = (size_t)(n - a0) * vsz, o1 = o0 + vsz;
+                k_adjb_cells<<<cb, 256, 0, s>>>(m.n_t, NS, ns, kmat, m.tets, m.comp, m.dof_of, m.n_comp, Lh, Ll,
+                                                sgh.p + o0, sgl.p + o0, sgh.p + o1, sgl.p + o1, th, accD, accT);
+                if (m.n_iface > 0)
+                    k_adjb_facets<<<fb, 256, 0, s>>>(m.n_iface, NS, ns, m.iface_cell, m.iface_face, m.xyz, m.tets,
+                                                     m.nbr, m.comp, m.dof_of, m.n_comp, Lh, Ll, sgh.p + o0,
+                                                     sgl.p + o0, sgh.p + o1, sgl.p + o1, th, accK);
+                BT_CUDA(cudaGetLastError());
+            }
+            if (a0 > 0) {   // lambda_{a0} starts the previous segment
+                BT_CUDA(cudaMemcpyAsync(lch.p, bkh.p + (size_t)(len - 1) * vsz, vsz * sizeof(float2),
+                                        cudaMemcpyDeviceToDevice, s));
+                BT_CUDA(cudaMemcpyAsync(lcl.p, bkl.p + (size_t)(len - 1) * vsz, vsz * sizeof(float2),
+                                        cudaMemcpyDeviceToDevice, s));
+            }
+        }
+        // per-signal sums over regions and region pairs, in a fixed order
+        red.alloc((size_t)NS * (2 * nr + nr * nr));
+        k_adjb_reduce<<<dim3(NS, nr), 256, 0, s>>>(m.n_t, NS, m.region, nr, accD, red.p);
+        k_adjb_reduce<<<dim3(NS, nr), 256, 0, s>>>(m.n_t, NS, m.region, nr, accT, red.p + (size_t)NS * nr);
+        if (m.n_iface > 0)
+            k_adjb_reduce<<<dim3(NS, nr * nr), 256, 0, s>>>(m.n_iface, NS, pair, nr * nr, accK,
+                                                           red.p + (size_t)2 * NS * nr);
+        BT_CUDA(cudaGetLastError());
+        std::vector<double> hr((size_t)NS * (2 * nr + nr * nr), 0.0);
+        red.download(hr.data(), (size_t)NS * (2 * nr + (m.n_iface > 0 ? nr * nr : 0)), s);
+        BT_CUDA(cudaStreamSynchronize(s));
+        for (int sg = 0; sg < NS; ++sg) {
+            const size_t o = (size_t)(b0 + sg);
+            for (int r = 0; r < nr; ++r) {
+                if (dD) dD[o * nr + r] = hr[(size_t)sg * nr + r];
+                if (dinvT2) dinvT2[o * nr + r] = hr[(size_t)NS * nr + (size_t)sg * nr + r];
+            }
+            if (dkappa)
+                for (int r1 = 0; r1 < nr; ++r1)
+                    for (int r2 = 0; r2 < nr; ++r2) {
+                        const int a = std::min(r1, r2), b = std::max(r1, r2);
+                        dkappa[o * nr * nr + (size_t)r1 * nr + r2] =
+                            (a == b) ? 0.0 : hr[(size_t)2 * NS * nr + (size_t)sg * nr * nr + (size_t)a * nr + b];
+                    }
+        }
+    }
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    BT_CUDA(cudaEventSynchronize(ctx->ev2));
+    float total = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&total, ctx->ev0, ctx->ev2));
+    if (st) {
+        st->gpu_ms = total;
+        st->stepper_ms = ms;
+        st->kernel_launches = launches;
+    }
 }
 
 }  // namespace bt

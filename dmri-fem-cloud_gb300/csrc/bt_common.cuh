@@ -228,6 +228,9 @@ void solve_mixed_multi(bt_ctx* const* ctxs, int32_t n_meshes, const int32_t* nsi
                        bt_stats* st);
 void reset_tuning_mixed(bt_ctx* ctx);
 void set_periodic(bt_ctx* ctx, const int32_t* dir);
+void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
+                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
+                   bt_stats* st);
 
 void free_solvers(bt_ctx* ctx);
 double device_sum(const double* d, int64_t n, cudaStream_t s);

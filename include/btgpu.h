@@ -217,6 +217,18 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
                double* signal_out, double* dS_dD, double* dS_dinvT2, double* dS_dkappa,
                bt_stats* stats);
 
+/* The same discrete adjoint for n_signals signals at once in the batched mixed
+ * precision stepper (FP32 Krylov vectors, double-float residuals; the backward
+ * sweep is a forward sweep of the same kernel with the schedule pair
+ * f_new[n-1], f_old[n]): signal_out[n_signals], dS_dD[n_signals*n_regions],
+ * dS_dinvT2[n_signals*n_regions], dS_dkappa[n_signals*n_regions*n_regions]
+ * (signal-major, as bt_adjoint per signal).  u0 = 1.  Up to 128 signals share
+ * one set of launches; more are processed in groups.  Any output pointer but
+ * signal_out may be NULL. */
+int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir,
+                     const int32_t* sequence, double rtol, int32_t max_iterations, int32_t checkpoint_stride,
+                     double* signal_out, double* dS_dD, double* dS_dinvT2, double* dS_dkappa, bt_stats* stats);
+
 /* Tangent-linear FP64 run: the signal and its derivative with respect to one
  * coefficient, param = BT_PARAM_D (D of region i), BT_PARAM_INVT2 (1/T2 of
  * region i) or BT_PARAM_KAPPA (permeability of the region pair (i, j)), by the

@@ -138,3 +138,23 @@ def test_tangent_linear_matches_adjoint(pkg, lib):
     again = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000)
     assert again["signal"] == adj["signal"]
     ctx.close()
+
+
+def test_batched_mixed_adjoint_matches_fp64(pkg, lib):
+    """bt_adjoint_batch (mixed precision, several signals in one set of launches,
+    the backward sweep run by the batched stepper) against the FP64 adjoint of
+    each signal: gradients within 1e-5 of their scale, signals within 1e-6."""
+    xyz, tets, reg, D, invT2, kp = layered_case(pkg, n=6)
+    ctx, q = make(pkg, xyz, tets, reg, D, invT2, kp)
+    qs = np.array([q, 0.7 * q, 1.2 * q])
+    gs = np.array([G, [1.0, 0.0, 0.0], [0.0, 0.6, 0.8]])
+    refs = [ctx.adjoint(qs[i], gs[i], rtol=1e-14, max_iterations=20000) for i in range(3)]
+    for stride in (0, 7):
+        out = ctx.adjoint_batch(qs, gs, rtol=1e-9, stride=stride)
+        for i, ref in enumerate(refs):
+            assert abs(out["signal"][i] - ref["signal"]) <= 1e-6 * abs(ref["signal"])
+            for k in ("dD", "dinvT2", "dkappa"):
+                scale = np.max(np.abs(ref[k]))
+                err = np.max(np.abs(out[k][i] - ref[k]))
+                assert err <= 1e-5 * scale, (stride, i, k, err / scale)
+    ctx.close()
