@@ -306,6 +306,7 @@ def gpu_run(args):
 
     batched = batched_leg(args, pkg, stream, flush, peak, peak_src) if args.batched_signals > 0 else None
     uneven = uneven_leg(args, pkg, stream, flush) if args.uneven_meshes > 0 else None
+    adjoint = adjoint_leg(args, pkg, stream, flush) if args.adjoint_signals > 0 else None
 
     # end to end through the public C-ABI from host buffers
     e2e_ms = []
@@ -349,6 +350,7 @@ def gpu_run(args):
             "plain_fp64": plain,
             "batched": batched,
             "uneven": uneven,
+            "adjoint": adjoint,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "signals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
@@ -422,6 +424,58 @@ def batched_leg(args, pkg, stream, flush, peak, peak_src):
                          "bytes_per_launch": byts, "launch_ms": st["stepper_ms"],
                          "peak_source": peak_src + " hbm_gbs (copy)",
                          "note": "algorithmic bytes (bench.alg_bytes_mixed); working set larger than L2"}}
+
+
+def adjoint_leg(args, pkg, stream, flush):
+    """Gradients: the layered-sphere 48^3 workload (4 layers, per-layer D and T2,
+    per-interface kappa), the first `adjoint_signals` of its 120 signals spread
+    evenly; the batched mixed-precision adjoint (bt_adjoint_batch, one set of
+    launches) against the FP64 adjoint of one signal (bt_adjoint), and the
+    gradient error of that signal."""
+    import torch
+    w = pkg.meshgen.workload("cfg4")
+    prof = w["profiles"]
+    fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in prof])
+    sig = w["signals"]
+    idx = np.linspace(0, len(sig) - 1, args.adjoint_signals).astype(int)
+    sel = [sig[i] for i in idx]
+    q = np.array([pkg.sequences.b_to_q(b, prof[pi].int4gb()) for b, _, pi in sel])
+    g = np.array([gd for _, gd, _ in sel], np.float64)
+    g /= np.linalg.norm(g, axis=1, keepdims=True)
+    ctx = pkg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    ctx.set_stream(stream.cuda_stream)
+    ctx.mesh_upload(w["xyz"], w["tets"], w["region"], w["n_regions"], None)
+    ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
+    ctx.assemble()
+    ctx.set_schedule(np.array(fns), np.array(fos), w["dt"])
+
+    def timed(fn_):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn_()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    ctx.solve(q, g, None, None, pkg.PRECISION_MIXED, 1e-9, args.maxit)          # warm-up (autotuner)
+    ms_b, out = timed(lambda: ctx.adjoint_batch(q, g, rtol=1e-9, max_iterations=args.maxit))
+    ms_64, ref = timed(lambda: ctx.adjoint(q[0], g[0], rtol=1e-12, max_iterations=args.maxit))
+    err = {k: float(np.max(np.abs(out[k][0] - ref[k])) / np.max(np.abs(ref[k])))
+           for k in ("dD", "dinvT2", "dkappa")}
+    info = ctx.info()
+    ctx.close()
+    n = len(q)
+    return {"workload": "layered sphere 48^3 (4 regions, D/T2 per layer, kappa per interface), PGSE, "
+                        "%d signals in one batched adjoint" % n,
+            "n_dofs": info["n_dofs"], "signals": n,
+            "batched_mixed": {"gradients_per_s": n / (ms_b / 1e3), "ms": ms_b,
+                              "parameters_per_signal": "D x4, 1/T2 x4, kappa x3"},
+            "fp64_one_signal": {"gradients_per_s": 1.0 / (ms_64 / 1e3), "ms": ms_64},
+            "ratio": (n / ms_b) / (1.0 / ms_64),
+            "max_rel_err_vs_fp64_adjoint": err,
+            "signal_rel_err": float(abs(out["signal"][0] - ref["signal"]) / abs(ref["signal"]))}
 
 
 def uneven_leg(args, pkg, stream, flush):
@@ -544,6 +598,8 @@ def main():
     ap.add_argument("--cpu-sample-steps-ref", type=int, default=6)
     ap.add_argument("--batched-profile", type=int, default=0,
                     help="only one short batched launch of this many steps, for a profiler")
+    ap.add_argument("--adjoint-signals", type=int, default=16,
+                    help="signals of the batched-adjoint leg on the 48^3 layered sphere (0: skip)")
     ap.add_argument("--uneven-meshes", type=int, default=16,
                     help="meshes of the uneven multi-mesh leg (0: skip)")
     ap.add_argument("--batched-signals", type=int, default=64,

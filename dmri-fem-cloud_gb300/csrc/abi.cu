@@ -475,6 +475,9 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
             BT_REQUIRE(iv >= -1 && iv <= 1, BT_ERR_INVALID, "mixed.reduce must be -1 (by size), 0 or 1");
             ctx->opt_mixed_reduce = iv;
             bt::reset_tuning_mixed(ctx);
+        } else if (k == "mixed.divergence") {
+            BT_REQUIRE(value >= 1.0, BT_ERR_INVALID, "mixed.divergence must be >= 1");
+            ctx->opt_mixed_growth2 = value * value;
         } else if (k == "mixed.extrapolate") {
             BT_REQUIRE(iv >= 0 && iv <= 2, BT_ERR_INVALID, "mixed.extrapolate must be 0, 1 or 2");
             ctx->opt_mixed_extrapolate = iv;

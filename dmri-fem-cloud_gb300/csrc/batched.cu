@@ -150,6 +150,7 @@ struct MixArgs {
     // discrete adjoint (adjoint_mixed): the first step's right-hand side is the
     // signal weight w (from a zero state), and the state after every save_every-th
     // step is copied to save_h / save_l [(step + 1) / save_every - 1][n][Rp/2]
+    float growth2;        // a slot ends its sweep when rr2 > growth2 * (smallest rr2 of the sweep)
     int32_t rhs_w;
     int32_t save_every;
     float2* save_h;
@@ -463,10 +464,33 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
     return true;
 }
 
+// (1 - theta) sum_e c_e exp(i ps g.shift_e) u_n[col_e] of one boundary row, in
+// FP64.  Kept out of line: its sincos (with the local array of the large-
+// argument reduction) would otherwise weigh on the register allocation of the
+// whole persistent kernel.
+__device__ __noinline__ double2 periodic_term(const MixArgs& a, int row, int r0, int c4, int Rp4, double ps) {
+    const double g0 = a.gvd[r0 * 3 + 0], g1 = a.gvd[r0 * 3 + 1], g2 = a.gvd[r0 * 3 + 2];
+    double bx = 0.0, by = 0.0;
+    for (int32_t e = a.per_ptr[row]; e < a.per_ptr[row + 1]; ++e) {
+        const PerVal v = a.per_val[e];
+        double sn, cs;
+        sincos(ps * (g0 * v.x + g1 * v.y + g2 * v.z), &sn, &cs);
+        const size_t ki = (size_t)a.per_col[e] * Rp4 + c4;
+        const float2 kh = a.uh[ki], kl = a.ul[ki];
+        const double ux = (double)kh.x + (double)kl.x, uy = (double)kh.y + (double)kl.y;
+        bx = fma(v.c, cs * ux - sn * uy, bx);
+        by = fma(v.c, sn * ux + cs * uy, by);
+    }
+    return make_double2((1.0 - a.theta_d) * bx, (1.0 - a.theta_d) * by);
+}
+
 // ------------------------------------------------------------------ kernel ----
 // The stepper on one mesh, run by blocks bid = 0..nb-1 of a (sub-)grid whose
 // blocks are all co-resident.
-template <int LPR>
+// kX: the optional paths (pseudo-periodic term, adjoint right-hand side w,
+// per-step state saves) are compiled only into the kX = true kernels, so the
+// plain stepper keeps the register allocation it has without them.
+template <int LPR, bool kX>
 __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bid, const unsigned nb) {
     constexpr int G = 32 / LPR;  // rows per warp-unit
     constexpr int C = 2 * LPR;   // RHS per warp-unit
@@ -576,31 +600,14 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             // -i cs (a + i b) = cs b - i cs a
             DF re = df_add(df_neg(df_norm(sr[0])), df_scale(jg[1], cs[0]));
             DF im = df_add(df_neg(df_norm(sr[1])), df_scale(jg[0], -cs[0]));
-            if (a.per_ptr) {
+            if (kX && a.per_ptr && a.per_ptr[row] < a.per_ptr[row + 1]) {
                 // pseudo-periodic mirror term of b, in FP64 (boundary rows only)
-                const int32_t pe0 = a.per_ptr[row], pe1 = a.per_ptr[row + 1];
-                if (pe0 < pe1) {
-                    const double ps = qd[0] * a.Fint[(size_t)sq[0] * a.sched_stride + step];
-                    const double g0 = a.gvd[r0 * 3 + 0], g1 = a.gvd[r0 * 3 + 1], g2 = a.gvd[r0 * 3 + 2];
-                    double bx = 0.0, by = 0.0;
-                    for (int32_t e = pe0; e < pe1; ++e) {
-                        const PerVal v = a.per_val[e];
-                        double sn, cs2;
-                        sincos(ps * (g0 * v.x + g1 * v.y + g2 * v.z), &sn, &cs2);
-                        const size_t ki = (size_t)a.per_col[e] * Rp4 + c4;
-                        const float2 kh = a.uh[ki], kl = a.ul[ki];
-                        const double ux = (double)kh.x + (double)kl.x, uy = (double)kh.y + (double)kl.y;
-                        bx = fma(v.c, cs2 * ux - sn * uy, bx);
-                        by = fma(v.c, sn * ux + cs2 * uy, by);
-                    }
-                    bx *= 1.0 - a.theta_d;
-                    by *= 1.0 - a.theta_d;
-                    const float bxh = (float)bx, byh = (float)by;
-                    re = df_add(re, DF{bxh, (float)(bx - (double)bxh)});
-                    im = df_add(im, DF{byh, (float)(by - (double)byh)});
-                }
+                const double2 bt = periodic_term(a, row, r0, c4, Rp4, qd[0] * a.Fint[(size_t)sq[0] * a.sched_stride + step]);
+                const float bxh = (float)bt.x, byh = (float)bt.y;
+                re = df_add(re, DF{bxh, (float)(bt.x - (double)bxh)});
+                im = df_add(im, DF{byh, (float)(bt.y - (double)byh)});
             }
-            if (a.rhs_w && step == 0) {   // b = w from the zero state: r = w
+            if (kX && a.rhs_w && step == 0) {   // b = w from the zero state: r = w
                 const double wv = a.w[row];
                 const float wh = (float)wv;
                 re = df_add(re, DF{wh, (float)(wv - (double)wh)});
@@ -699,7 +706,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             kadd(red[1][0], im.h * z1.x);
             kadd(red[1][1], im.h * z1.y);
             kadd(red[1][2], im.h * im.h);
-            const float bn = (a.rhs_w && step == 0) ? (float)(a.w[row] * a.w[row])
+            const float bn = (kX && a.rhs_w && step == 0) ? (float)(a.w[row] * a.w[row])
                                                     : wr * wr * (uhr.x * uhr.x + uhr.y * uhr.y);
             kadd(red[0][3], bn);
             kadd(red[1][3], bn);
@@ -721,6 +728,11 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             // ---- inner FP32 Jacobi-COCG on A d = r (sweep start residual rrs)
             const float eps = (sweep == 0) ? a.eps_first : a.eps_next;
             float2 beta[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            // smallest residual of the sweep: a slot whose FP32 COCG residual grows 100x
+            // (in norm) above it is diverging (a near-breakdown of the unconjugated
+            // form) and ends its sweep; the double-float phase U then measures the true
+            // residual and the next sweep restarts from it
+            float rrmin[2] = {rr2[0], rr2[1]};
             bool act[2];
             int it = 0;
             while (true) {
@@ -730,7 +742,8 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 // next decision can race with a slow warp still reading the previous one.
 #pragma unroll
                 for (int j = 0; j < 2; ++j)
-                    act[j] = (r0 + j < a.R) && rr2[j] > eps * eps * rrs[j] && rr2[j] > 0.09f * tolb2[j];
+                    act[j] = (r0 + j < a.R) && rr2[j] > eps * eps * rrs[j] && rr2[j] > 0.09f * tolb2[j] &&
+                             rr2[j] <= a.growth2 * rrmin[j];
                 if (!__syncthreads_or(act[0] || act[1])) break;
                 if (it >= a.maxit) {
                     if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
@@ -928,6 +941,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                     if (act[j]) {
                         rho[j] = rn2;
                         rr2[j] = rbs[j][2];
+                        rrmin[j] = fminf(rrmin[j], rr2[j]);
                     }
                 }
                 ++it;
@@ -1043,7 +1057,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             a.sweeps[step] = sweep;
         }
         if (failed) return;
-        if (a.save_h && (step + 1) % a.save_every == 0) {
+        if (kX && a.save_h && (step + 1) % a.save_every == 0) {
             // every lane copies its own (row, signal) entries, which it wrote itself in phase U
             const size_t off = (size_t)((step + 1) / a.save_every - 1) * a.n * Rp4;
             for (int g = g0; g < gend; g += gstride) {
@@ -1104,15 +1118,15 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
     }
 }
 
-template <int LPR>
+template <int LPR, bool kX>
 __global__ void __maxnreg__(120) k_batched(MixArgs a) {
-    batched_body<LPR>(a, blockIdx.x, gridDim.x);
+    batched_body<LPR, kX>(a, blockIdx.x, gridDim.x);
 }
 
 // Several meshes in one cooperative launch: blocks first[m] .. first[m+1]-1 form
 // the sub-grid of mesh m, which runs its own stepper with its own barrier
 // counters and reductions; meshes never wait for one another.
-template <int LPR>
+template <int LPR, bool kX>
 __global__ void __maxnreg__(120) k_batched_multi(const MixArgs* __restrict__ args, const int* __restrict__ first,
                                                  int n_meshes) {
     __shared__ MixArgs s_a;
@@ -1125,7 +1139,7 @@ __global__ void __maxnreg__(120) k_batched_multi(const MixArgs* __restrict__ arg
     }
     __syncthreads();
     const int m = s_m;
-    batched_body<LPR>(s_a, blockIdx.x - first[m], first[m + 1] - first[m]);
+    batched_body<LPR, kX>(s_a, blockIdx.x - first[m], first[m + 1] - first[m]);
 }
 
 // Pack the double-float matrix copies and the row data once per assembly/theta/dt.
@@ -1179,26 +1193,34 @@ namespace {
 using KFn = void (*)(MixArgs);
 using KFnMulti = void (*)(const MixArgs*, const int*, int);
 
-KFnMulti kernel_multi_for(int lpr) {
+template <bool kX>
+KFnMulti kernel_multi_lpr(int lpr) {
     switch (lpr) {
-        case 1: return k_batched_multi<1>;
-        case 2: return k_batched_multi<2>;
-        case 4: return k_batched_multi<4>;
-        case 8: return k_batched_multi<8>;
-        case 16: return k_batched_multi<16>;
-        default: return k_batched_multi<32>;
+        case 1: return k_batched_multi<1, kX>;
+        case 2: return k_batched_multi<2, kX>;
+        case 4: return k_batched_multi<4, kX>;
+        case 8: return k_batched_multi<8, kX>;
+        case 16: return k_batched_multi<16, kX>;
+        default: return k_batched_multi<32, kX>;
     }
 }
 
-KFn kernel_for(int lpr) {
+template <bool kX>
+KFn kernel_lpr(int lpr) {
     switch (lpr) {
-        case 1: return k_batched<1>;
-        case 2: return k_batched<2>;
-        case 4: return k_batched<4>;
-        case 8: return k_batched<8>;
-        case 16: return k_batched<16>;
-        default: return k_batched<32>;
+        case 1: return k_batched<1, kX>;
+        case 2: return k_batched<2, kX>;
+        case 4: return k_batched<4, kX>;
+        case 8: return k_batched<8, kX>;
+        case 16: return k_batched<16, kX>;
+        default: return k_batched<32, kX>;
     }
+}
+
+KFn kernel_for(int lpr, bool extras) { return extras ? kernel_lpr<true>(lpr) : kernel_lpr<false>(lpr); }
+
+KFnMulti kernel_multi_for(int lpr, bool extras) {
+    return extras ? kernel_multi_lpr<true>(lpr) : kernel_multi_lpr<false>(lpr);
 }
 
 int ceil_pow2(int v) {
@@ -1300,6 +1322,7 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
         a.Fint = P.on ? W.Fint.p : nullptr;
         a.gvd = W.gvd.p;
         a.theta_d = S.theta;
+        a.growth2 = (float)ctx->opt_mixed_growth2;
         a.rhs_w = 0;
         a.save_every = 1;
         a.save_h = nullptr;
@@ -1410,7 +1433,7 @@ struct MixExtra {
 static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int blocked, int n_steps,
                           double rtol, int maxit, const double* d_u0, const MixExtra* ex = nullptr) {
     cudaStream_t s = ctx->stream;
-    KFn fn = kernel_for(lpr);
+    KFn fn = kernel_for(lpr, ctx->per.on || (ex && (ex->rhs_w || ex->save_h)));
     int occ = 0;
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
     BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
@@ -1680,7 +1703,9 @@ static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R
                           double rtol, int maxit, const std::vector<const double*>& d_u0) {
     bt_ctx* c0 = ctxs[0];
     cudaStream_t s = c0->stream;
-    KFnMulti fn = kernel_multi_for(lpr);
+    bool extras = false;
+    for (int m = 0; m < nm; ++m) extras = extras || ctxs[m]->per.on;
+    KFnMulti fn = kernel_multi_for(lpr, extras);
     int occ = 0;
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
     BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");

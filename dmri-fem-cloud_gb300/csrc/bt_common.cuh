@@ -200,7 +200,8 @@ struct bt_ctx {
     double opt_mixed_eps_next = 1e-2;
     int opt_mixed_extrapolate = 2;
     int opt_mixed_blocked = -1;
-    int opt_mixed_reduce = -1;   // grid sums of the mixed stepper: -1 by size, 0 last block, 1 every block
+    int opt_mixed_reduce = -1;
+    double opt_mixed_growth2 = 1e8;   // divergence guard of a sweep (squared-norm growth over its minimum)   // grid sums of the mixed stepper: -1 by size, 0 last block, 1 every block
     int opt_fp64_extrapolate = 1;
 };
 

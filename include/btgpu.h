@@ -250,6 +250,8 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *   "mixed.eps_first"       inner FP32 tolerance of the first sweep (3e-6)
  *   "mixed.eps_next"        inner FP32 tolerance of later sweeps (1e-2)
  *   "mixed.blocked_rows"    rows of a block: 1 contiguous range, 0 interleaved, -1 tuned (default)
+ *   "mixed.divergence"      an FP32 inner sweep of a signal ends when its residual norm grows this
+ *                           many times above the smallest it reached in the sweep (default 1e4)
  *   "mixed.reduce"          grid sums: 0 the last block to arrive sums and publishes, 1 every block sums
  *                           all partials itself, -1 by size (default; same bits either way)
  *   "mixed.extrapolate"     initial guess of each step: 2 = 3u_n - 3u_{n-1} + u_{n-2} (default),
