@@ -728,11 +728,15 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             // ---- inner FP32 Jacobi-COCG on A d = r (sweep start residual rrs)
             const float eps = (sweep == 0) ? a.eps_first : a.eps_next;
             float2 beta[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-            // smallest residual of the sweep: a slot whose FP32 COCG residual grows 100x
-            // (in norm) above it is diverging (a near-breakdown of the unconjugated
-            // form) and ends its sweep; the double-float phase U then measures the true
-            // residual and the next sweep restarts from it
+            // smallest residual of the sweep: a slot whose FP32 COCG residual grows
+            // a.growth2 times above it (squared norms) is diverging (a near-breakdown of
+            // the unconjugated form), and a slot whose residual has not halved (in
+            // norm) for 64 iterations has reached FP32's attainable accuracy; either
+            // ends its sweep, the double-float phase U measures the true residual and
+            // the next sweep restarts from it
             float rrmin[2] = {rr2[0], rr2[1]};
+            float rrmark[2] = {rr2[0], rr2[1]};
+            int itmark[2] = {0, 0};
             bool act[2];
             int it = 0;
             while (true) {
@@ -743,7 +747,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
 #pragma unroll
                 for (int j = 0; j < 2; ++j)
                     act[j] = (r0 + j < a.R) && rr2[j] > eps * eps * rrs[j] && rr2[j] > 0.09f * tolb2[j] &&
-                             rr2[j] <= a.growth2 * rrmin[j];
+                             rr2[j] <= a.growth2 * rrmin[j] && it - itmark[j] < 64;
                 if (!__syncthreads_or(act[0] || act[1])) break;
                 if (it >= a.maxit) {
                     if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
@@ -942,6 +946,10 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                         rho[j] = rn2;
                         rr2[j] = rbs[j][2];
                         rrmin[j] = fminf(rrmin[j], rr2[j]);
+                        if (rr2[j] < 0.25f * rrmark[j]) {
+                            rrmark[j] = rr2[j];
+                            itmark[j] = it + 1;
+                        }
                     }
                 }
                 ++it;
