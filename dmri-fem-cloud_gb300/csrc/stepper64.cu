@@ -636,7 +636,7 @@ void free_solver64(bt_ctx* ctx) {
 namespace bt {
 
 // ============================================================== adjoint ====
-// Discrete adjoint of the FP64 Crank-Nicolson loop (spec form (3)).
+// Discrete adjoint of the FP64 Crank-Nicolson loop.
 //
 //   forward   A_n u_{n+1} = B_n u_n,   Sig = Re(w^T u_N)
 //   adjoint   lambda_N = A_{N-1}^{-1} w,  lambda_n = A_{n-1}^{-1} B_n lambda_{n+1}

@@ -29,7 +29,7 @@ closed-form P1 integrals below agree with DOLFIN up to rounding:
 * facet mass      int_F phi_i phi_j       = A/12 (1 + delta_ij)
 
 Interface permeability ``kappa``: ``kappa_mode='facet'`` uses one value per
-facet, taken from the region pair of its two cells (the north-star form);
+facet, taken from the region pair of its two cells (the engine's form);
 ``kappa_mode='cr'`` reproduces the Crouzeix-Raviart field of
 ``MultilayeredDiskVariablePermeability.ipynb:480-502`` (facet dof = the pair
 value on interface facets, 0 elsewhere; ``avg(kappa)`` integrated exactly).
