@@ -67,3 +67,33 @@ def test_mirror_map_of_matching_faces():
     cells, fv = exterior_facets(tets)
     assert len(fv) == 6 * 4 * 4 * 2
     assert np.allclose(per["B"].toarray(), per["B"].toarray().T)
+
+
+def test_mirror_map_two_compartments():
+    """Across the z faces of a box with a z-cylinder every boundary dof mirrors to
+    the opposite vertex, with weight 1, in its own compartment -- or to nothing
+    when that vertex has no dof in the compartment (the Kuhn split is not mirror-
+    symmetric in z, so the centroid staircase of the cylinder differs slightly
+    between the two faces)."""
+    xyz, tets = oracle.box_mesh([-L, -L, -L], [L, L, L], 6)
+    mid = xyz[tets].mean(axis=1)
+    reg = (mid[:, 0] ** 2 + mid[:, 1] ** 2 < 2.5 ** 2).astype(np.int64)
+    sysd = forms.duplicated_system(xyz, tets, reg, [D, D], 0.0, np.array([[0.0, 1e-5], [1e-5, 0.0]]))
+    dof = sysd["dof"]
+    per = weak_periodic(xyz, tets, reg % 2, dof, [0, 0, 1])
+    on_face = np.abs(np.abs(xyz[:, 2]) - L) < 1e-9
+    assert len(per["mirror"]) == int(sum((dof[v] >= 0).sum() for v in np.nonzero(on_face)[0]))
+    where = {tuple(np.round(p, 9)): v for v, p in enumerate(xyz)}
+    matched = empty = 0
+    for j, (ks, ws, shift) in per["mirror"].items():
+        v, c = sysd["vertex"][j], sysd["field"][j]
+        target = xyz[v].copy()
+        target[2] = -target[2]
+        w = where[tuple(np.round(target, 9))]
+        if dof[w, c] >= 0:
+            assert list(ks) == [dof[w, c]] and ws[0] == 1.0
+            matched += 1
+        else:
+            assert len(ks) == 0
+            empty += 1
+    assert matched > 10 * empty and sum(int((dof[v] >= 0).sum() == 2) for v in np.nonzero(on_face)[0]) > 0
