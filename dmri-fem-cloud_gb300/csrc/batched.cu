@@ -2140,7 +2140,6 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
     float ms = 0.0f;
     int64_t launches = 1;
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
-    std::vector<double> hD, hT, hK;
     for (int32_t b0 = 0; b0 < nsig; b0 += kMaxRhs / 2) {
         const int NS = std::min<int32_t>(kMaxRhs / 2, nsig - b0);
         const int R = 2 * NS;
