@@ -31,6 +31,10 @@ def test_null_arguments_are_rejected(lib):
     assert lib.bt_solve(None, 1, None, None, None, None, 0, 1e-9, 10, None, None, None, None) == 1
     buf = ctypes.create_string_buffer(8)
     assert lib.bt_last_error(None, buf, 8) == 1
+    assert lib.bt_set_periodic(None, None) == 1
+    assert lib.bt_periodic_info(None, None) == 1
+    assert lib.bt_set_schedule_phase(None, None, 1, 1) == 1
+    assert lib.bt_adjoint_batch(None, 1, None, None, None, 1e-9, 10, 0, None, None, None, None, None) == 1
 
 
 def test_no_cpu_fallback_without_library(pkg, tmp_path, monkeypatch):
