@@ -1932,9 +1932,10 @@ void free_solver_mixed(bt_ctx* ctx) {
 // states are recomputed segment by segment from checkpoints every stride steps.
 namespace {
 
-// per-cell gradient products: upper triangle of grad(phi_r).grad(phi_c) * vol, and vol
-__global__ void k_cell_kmat(int64_t n_t, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
-                            double* __restrict__ kmat) {
+// per-cell geometry: the gradients G_1..G_3 of the barycentric coordinates of
+// vertices 1..3 (G_0 = -(G_1 + G_2 + G_3)) and the volume, as 12 floats
+__global__ void k_cell_grad(int64_t n_t, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                            float4* __restrict__ geo) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_t) return;
     double X[4][3];
@@ -1952,33 +1953,31 @@ __global__ void k_cell_kmat(int64_t n_t, const double* __restrict__ xyz, const i
     const double c02 = E[1][0] * E[2][1] - E[1][1] * E[2][0];
     const double det = E[0][0] * c00 + E[0][1] * c01 + E[0][2] * c02;
     const double id = 1.0 / det;
-    double G[4][3];
-    G[1][0] = c00 * id; G[1][1] = c01 * id; G[1][2] = c02 * id;
-    G[2][0] = (E[0][2] * E[2][1] - E[0][1] * E[2][2]) * id;
-    G[2][1] = (E[0][0] * E[2][2] - E[0][2] * E[2][0]) * id;
-    G[2][2] = (E[0][1] * E[2][0] - E[0][0] * E[2][1]) * id;
-    G[3][0] = (E[0][1] * E[1][2] - E[0][2] * E[1][1]) * id;
-    G[3][1] = (E[0][2] * E[1][0] - E[0][0] * E[1][2]) * id;
-    G[3][2] = (E[0][0] * E[1][1] - E[0][1] * E[1][0]) * id;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) G[0][c] = -(G[1][c] + G[2][c] + G[3][c]);
-    const double vol = fabs(det) / 6.0;
-    int k = 0;
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = r; c < 4; ++c)
-            kmat[t * 11 + k++] = vol * (G[r][0] * G[c][0] + G[r][1] * G[c][1] + G[r][2] * G[c][2]);
-    kmat[t * 11 + 10] = vol;
+    const double g[9] = {c00 * id, c01 * id, c02 * id,
+                         (E[0][2] * E[2][1] - E[0][1] * E[2][2]) * id,
+                         (E[0][0] * E[2][2] - E[0][2] * E[2][0]) * id,
+                         (E[0][1] * E[2][0] - E[0][0] * E[2][1]) * id,
+                         (E[0][1] * E[1][2] - E[0][2] * E[1][1]) * id,
+                         (E[0][2] * E[1][0] - E[0][0] * E[1][2]) * id,
+                         (E[0][0] * E[1][1] - E[0][1] * E[1][0]) * id};
+    geo[t * 3 + 0] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)g[3]);
+    geo[t * 3 + 1] = make_float4((float)g[4], (float)g[5], (float)g[6], (float)g[7]);
+    geo[t * 3 + 2] = make_float4((float)g[8], (float)(fabs(det) / 6.0), 0.0f, 0.0f);
 }
 
-__device__ __forceinline__ double2 state_at(const float2* __restrict__ h, const float2* __restrict__ l, size_t i) {
-    const float2 a = h[i], b = l[i];
-    return make_double2((double)a.x + (double)b.x, (double)a.y + (double)b.y);
+// x_k - x_0 of a double-float (hi, lo) state: the hi parts of nearby values
+// subtract exactly, the lo parts restore the digits the difference needs
+__device__ __forceinline__ float2 df_diff(const float2* __restrict__ h, const float2* __restrict__ l, size_t ik,
+                                          size_t i0) {
+    const float2 hk = h[ik], h0 = h[i0], lk = l[ik], l0 = l[i0];
+    return make_float2((hk.x - h0.x) + (lk.x - l0.x), (hk.y - h0.y) + (lk.y - l0.y));
 }
 
-// accD[t][s] -= Re(L^T K V), accT[t][s] -= Re(L^T M V) of cell t, signal s (unit coefficients)
-__global__ void k_adjb_cells(int64_t n_t, int NS, int ns, const double* __restrict__ kmat,
+// accD[t][s] -= Re(L^T K V), accT[t][s] -= Re(L^T M V) of cell t, signal s (unit
+// coefficients).  L^T K V = vol grad(L) . grad(V) with the gradients formed from
+// vertex differences (the rows of K sum to zero, so products of the raw vertex
+// values would cancel); M = vol/20 (1 + delta_rc).  FP32 products, FP64 sums.
+__global__ void k_adjb_cells(int64_t n_t, int NS, int ns, const float4* __restrict__ geo,
                              const int32_t* __restrict__ tets, const int32_t* __restrict__ comp,
                              const int32_t* __restrict__ dof_of, int nc, const float2* __restrict__ lh,
                              const float2* __restrict__ ll, const float2* __restrict__ u0h,
@@ -1990,30 +1989,50 @@ __global__ void k_adjb_cells(int64_t n_t, int NS, int ns, const double* __restri
     const int64_t t = idx / NS;
     const int sg = (int)(idx % NS);
     const int f = comp[t];
-    double2 L[4], V[4];
+    size_t i[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) i[k] = (size_t)dof_of[(int64_t)tets[t * 4 + k] * nc + f] * ns + sg;
+    const float th = (float)theta, om = (float)(1.0 - theta);
+    const float4 a = geo[t * 3 + 0], b = geo[t * 3 + 1], c = geo[t * 3 + 2];
+    const float G[3][3] = {{a.x, a.y, a.z}, {a.w, b.x, b.y}, {b.z, b.w, c.x}};
+    const float vol = c.y;
+    float2 gl[3], gv[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) gl[d] = gv[d] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        const float2 dl = df_diff(lh, ll, i[k], i[0]);
+        const float2 d0 = df_diff(u0h, u0l, i[k], i[0]), d1 = df_diff(u1h, u1l, i[k], i[0]);
+        const float2 dv = make_float2(th * d1.x + om * d0.x, th * d1.y + om * d0.y);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            gl[d].x = fmaf(dl.x, G[k - 1][d], gl[d].x);
+            gl[d].y = fmaf(dl.y, G[k - 1][d], gl[d].y);
+            gv[d].x = fmaf(dv.x, G[k - 1][d], gv[d].x);
+            gv[d].y = fmaf(dv.y, G[k - 1][d], gv[d].y);
+        }
+    }
+    float sK = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) sK += gl[d].x * gv[d].x - gl[d].y * gv[d].y;
+    float2 sl = make_float2(0.f, 0.f), sv = sl;
+    float sd = 0.f;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const size_t i = (size_t)dof_of[(int64_t)tets[t * 4 + k] * nc + f] * ns + sg;
-        L[k] = state_at(lh, ll, i);
-        const double2 a0 = state_at(u0h, u0l, i), a1 = state_at(u1h, u1l, i);
-        V[k] = make_double2(theta * a1.x + (1.0 - theta) * a0.x, theta * a1.y + (1.0 - theta) * a0.y);
+        const float2 L = lh[i[k]], A0 = u0h[i[k]], A1 = u1h[i[k]];
+        const float2 V = make_float2(th * A1.x + om * A0.x, th * A1.y + om * A0.y);
+        sl.x += L.x; sl.y += L.y;
+        sv.x += V.x; sv.y += V.y;
+        sd += L.x * V.x - L.y * V.y;
     }
-    const double* km = kmat + t * 11;
-    const double vol = km[10];
-    double sK = 0.0, sM = 0.0;
-    int k = 0;
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = r; c < 4; ++c) {
-            // symmetric: (r, c) and (c, r) together
-            const double re = L[r].x * V[c].x - L[r].y * V[c].y +
-                              (r == c ? 0.0 : L[c].x * V[r].x - L[c].y * V[r].y);
-            sK += km[k++] * re;
-            sM += (r == c ? vol / 10.0 : vol / 20.0) * re;
-        }
-    accD[idx] -= sK;
-    accT[idx] -= sM;
+    const float sM = (vol / 20.0f) * (sl.x * sv.x - sl.y * sv.y + sd);
+    accD[idx] -= (double)(vol * sK);
+    accT[idx] -= (double)sM;
+}
+
+__device__ __forceinline__ double2 state_at(const float2* __restrict__ h, const float2* __restrict__ l, size_t i) {
+    const float2 a = h[i], b = l[i];
+    return make_double2((double)a.x + (double)b.x, (double)a.y + (double)b.y);
 }
 
 // accK[i][s] -= Re([L]^T B [V]) of interface facet i (facet mass, jumps across the duplicated dofs)
@@ -2111,11 +2130,12 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
             afn[(size_t)r * N + j] = S.f_new[(size_t)r * N + N - 1 - j];
             if (j >= 1) afo[(size_t)r * N + j] = S.f_old[(size_t)r * N + N - j];
         }
-    DevBuf<double> d_afn, d_afo, kmat, accD, accT, accK, red;
+    DevBuf<double> d_afn, d_afo, accD, accT, accK, red;
+    DevBuf<float4> cgeo;
     d_afn.upload(afn.data(), afn.size(), s);
     d_afo.upload(afo.data(), afo.size(), s);
-    kmat.alloc((size_t)m.n_t * 11);
-    k_cell_kmat<<<(unsigned)((m.n_t + 127) / 128), 128, 0, s>>>(m.n_t, m.xyz, m.tets, kmat);
+    cgeo.alloc((size_t)m.n_t * 3);
+    k_cell_grad<<<(unsigned)((m.n_t + 127) / 128), 128, 0, s>>>(m.n_t, m.xyz, m.tets, cgeo);
     BT_CUDA(cudaGetLastError());
     // interface facet -> region pair (r1 <= r2) index r1 * nr + r2
     std::vector<int32_t> hreg(m.n_t), hpair(std::max<int64_t>(1, m.n_iface), 0);
@@ -2214,7 +2234,7 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
                 const float2* Lh = (n + 1 == e0) ? lch.p : bkh.p + (size_t)(e0 - 2 - n) * vsz;
                 const float2* Ll = (n + 1 == e0) ? lcl.p : bkl.p + (size_t)(e0 - 2 - n) * vsz;
                 const size_t o0 = (size_t)(n - a0) * vsz, o1 = o0 + vsz;
-                k_adjb_cells<<<cb, 256, 0, s>>>(m.n_t, NS, ns, kmat, m.tets, m.comp, m.dof_of, m.n_comp, Lh, Ll,
+                k_adjb_cells<<<cb, 256, 0, s>>>(m.n_t, NS, ns, cgeo, m.tets, m.comp, m.dof_of, m.n_comp, Lh, Ll,
                                                 sgh.p + o0, sgl.p + o0, sgh.p + o1, sgl.p + o1, th, accD, accT);
                 if (m.n_iface > 0)
                     k_adjb_facets<<<fb, 256, 0, s>>>(m.n_iface, NS, ns, m.iface_cell, m.iface_face, m.xyz, m.tets,
