@@ -1,33 +1,41 @@
 """Benchmark: Bloch-Torrey signals/s on one GB300 (contract: one JSON line).
 
-Workload (default): the two-compartment permeable box -- [-10,10]^3 um, 40^3
-Kuhn-split cubes (384,000 tets), inner compartment = cells with centroid
-x^2 + y^2 < 36 (interface nodes duplicated), D = 3e-3 um^2/us in both,
-kappa = 1e-5 um/us, PGSE delta = 10600 us, Delta = 43100 us, dt = 200 us
-(270 Crank-Nicolson steps), b in {1000, 3000} s/mm^2, gdir (0,1,0), u0 = 1.
-All inputs are synthetic and deterministic (seed 0).
+Headline (``value``): the plain FP64 path on the two-compartment permeable box,
+the configuration stated as plain FP64 -- [-10,10]^3 um, 40^3 Kuhn-split cubes
+(384,000 tets), inner compartment = cells with centroid x^2 + y^2 < 36
+(interface nodes duplicated), D = 3e-3 um^2/us in both, kappa = 1e-5 um/us,
+PGSE delta = 10600 us, Delta = 43100 us, dt = 200 us (270 Crank-Nicolson
+steps), b in {1000, 3000} s/mm^2, gdir (0,1,0), u0 = 1.  A "step" is one pass
+of the hot path over the batch: both signals integrated over all 270 time
+steps by libbtgpu's FP64 stepper (COCG to ||r|| <= 1e-12 ||b|| per step), mesh
+resident and assembled.  Each signal's error against the oracle's committed
+SuperLU solution of the same workload (tests/golden/oracle_signals.json) is
+printed in the line.  ``e2e`` repeats the measurement through the public C-ABI
+calls from host buffers (mesh upload and device graph build, coefficient
+upload, assembly, schedule, solve, signals back to the host).
 
-A "step" is one pass of the hot path over the whole batch: every signal of the
-workload integrated over all 270 time steps by libbtgpu.  ``value`` is the
-batched mixed-precision path (FP32 inner Jacobi-COCG, double-float residuals,
-outer rtol 1e-9; its signals agree with the FP64 path to <= 1e-6, checked in
-the line as ``plain_fp64.max_rel_err_mixed_vs_fp64``), measured with the mesh
-already resident and assembled; ``plain_fp64`` times the FP64 path (rtol 1e-12,
-the reference-parity path) on the same workload.  ``e2e`` repeats the
-measurement through the public C-ABI calls from host buffers (mesh upload and
-device graph build, coefficient upload, assembly, schedule, solve, signals back
-to the host).
+Legs (each its own timed region, named workload, precision and error):
 
-``batched`` is the batched form on the eight-cylinder 64^3 workload: 64 of its
-512 signals (Fibonacci directions x b-values, PGSE and cos-OGSE) in one
-mixed-precision launch against the FP64 path on two of the same signals.
-
-``uneven`` runs 16 small meshes of uneven size in one persistent launch
-(bt_solve_multi) against one launch per mesh.
+* ``mixed_cfg2``: the batched mixed-precision path (FP32 inner Jacobi-COCG on
+  Re/Im right-hand sides, double-float residuals and refinement, FP64 signal)
+  on the same 40^3 workload, its error per signal against the oracle and its
+  ratio to the FP64 path;
+* ``batched``: the eight-cylinder 64^3 workload with all 512 signals (64
+  Fibonacci directions x 8 b-values, PGSE and cos-OGSE) in two 256-signal
+  launches, against the FP64 path timed on signals spread over the 512; the
+  mixed-vs-FP64 error of every signal (the FP64 values of all 512 are the
+  committed fixture tests/golden/gpu_fp64_cfg3_signals.json, written by the FP64
+  path on a GB300, which is pinned to the oracle at 1e-9; the spread sample is
+  re-checked live);
+* ``uneven``: 16 small meshes of uneven size in one persistent launch
+  (bt_solve_multi) against one launch per mesh;
+* ``adjoint``: batched mixed-precision gradients on the 48^3 layered sphere
+  against the FP64 adjoint.
 
 ``--impl reference`` times the CPU restatement of the reference's solve path
-(two-field real system, Jacobi-BiCGSTAB rtol 1e-9 as GCloudDmriSolver.py
-ships it) with one process per host core, on a bounded sample of time steps.
+(two-field real system, Jacobi-BiCGSTAB rtol 1e-9 as GCloudDmriSolver.py ships
+it): one whole 270-step signal per process, set-up included, one process per
+host core.
 """
 
 import argparse
@@ -47,15 +55,19 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 PKG = "dmri-fem-cloud_gb300"
+METRIC = "Bloch-Torrey signals/s on 1 GB300 at ≤1e-6 rel err, batched vs plain FP64; HBM %"
+L2_BYTES = 129e6          # GB300 L2
 
 WORKLOADS = {
-    "cfg1": "one compartment, [-10,10]^3 um box, 20^3 Kuhn cubes (48,000 tets), D=3e-3, PGSE 10600/43100 us, "
-            "b=1000, gdir (1,0,0), dt=200 us",
-    "cfg2": "two compartments, [-10,10]^3 um box, 40^3 Kuhn cubes (384,000 tets), cylinder x^2+y^2<36, "
-            "D=3e-3, kappa=1e-5, PGSE 10600/43100 us, b in {1000,3000}, gdir (0,1,0), dt=200 us",
-    "cfg3": "eight seeded non-overlapping z-cylinders (radii U[2,5]) in a [-15,15]^3 um box, 64^3 Kuhn cubes "
-            "(1.57M tets), kappa=5e-5, D=3e-3, 64 Fibonacci directions x 8 b in [500,4000] = 512 signals, "
-            "directions 0-31 PGSE 10600/43100 us, 32-63 cos-OGSE (one period over delta), dt=200 us",
+    "cfg1": "plain FP64, one compartment, [-10,10]^3 um box, 20^3 Kuhn cubes (48,000 tets), D=3e-3, "
+            "PGSE 10600/43100 us, b=1000, gdir (1,0,0), dt=200 us",
+    "cfg2": "plain FP64 two-compartment permeable: [-10,10]^3 um box, 40^3 Kuhn cubes (384,000 tets), "
+            "cylinder x^2+y^2<36 (staircase, interface nodes duplicated), D=3e-3 both, kappa=1e-5, Neumann, "
+            "PGSE 10600/43100 us, b in {1000,3000}, gdir (0,1,0), dt=200 us, u0=1",
+    "cfg3": "batched + mixed precision: eight seeded non-overlapping z-cylinders (radii U[2,5]) in a "
+            "[-15,15]^3 um box, 64^3 Kuhn cubes (1.57M tets), kappa=5e-5, D=3e-3, 64 Fibonacci directions x 8 b "
+            "in [500,4000] = 512 signals, directions 0-31 PGSE 10600/43100 us, 32-63 cos-OGSE (one period over "
+            "delta), dt=200 us",
 }
 
 
@@ -144,47 +156,136 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def load_json(*parts):
+    path = os.path.join(ROOT, *parts)
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        return json.load(fh)
+
+
+def peak_hbm():
+    pk = load_json("MEASURED_PEAKS.json")
+    if pk and "hbm_gbs" in pk:
+        return float(pk["hbm_gbs"]), "measured hbm_gbs (copy), MEASURED_PEAKS.json"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def golden_cfg2():
+    """Oracle normalised signals of the full 40^3 workload, keyed by b."""
+    g = load_json("tests", "golden", "oracle_signals.json")
+    for case in (g or {}).get("cases", []):
+        if case["workload"] == "cfg2" and case["n"] is None:
+            return {float(s["b"]): s["normalized"] for s in case["signals"]}
+    return {}
+
+
 # ---------------------------------------------------------------- CPU legs ---
-def _cpu_sample_worker(args):
-    """One bounded sample: `steps` time steps of one signal of the workload on
-    the CPU restatement (literal two-field system, Jacobi-BiCGSTAB rtol 1e-9)."""
-    name, steps, sig_index = args
+def _cpu_signal_worker(args):
+    """One whole signal on the CPU restatement of the reference's solve path:
+    the literal two-field system (set-up: mesh + assembly of the forms, as one
+    GCloudDmriSolver.py job does) and all 270 Crank-Nicolson steps with
+    Jacobi-BiCGSTAB rtol 1e-9 / atol 1e-10 (GCloudDmriSolver.py:219-222)."""
+    name, sig_index = args
     sys.path.insert(0, ROOT)
     import oracle
     pkg = importlib.import_module(PKG)
+    t0 = time.perf_counter()
     w = pkg.meshgen.workload(name)
     s2 = oracle.two_field_system(w["xyz"], w["tets"], w["region"], np.asarray(w["D"]), 0.0, w["kappa"] or 0.0,
                                  multiple=w["multiple"])
     b, g, _ = w["signals"][sig_index % len(w["signals"])]
     prof = oracle.PGSE(10600, 43100)
     q = oracle.bvalue_to_q(b, prof.int4gb())
-    r = oracle.solve_two_field(s2, prof, q, g, w["dt"], solver="bicgstab", rtol=1e-9, atol=1e-10,
-                               max_steps=steps)
-    return r.elapsed, r.steps
+    t1 = time.perf_counter()
+    r = oracle.solve_two_field(s2, prof, q, g, w["dt"], solver="bicgstab", rtol=1e-9, atol=1e-10)
+    t2 = time.perf_counter()
+    it = np.asarray(r.iterations)
+    return {"setup_s": t1 - t0, "solve_s": t2 - t1, "steps": r.steps, "normalized": r.normalized, "b": b,
+            "iterations": [float(it[:53].mean()), float(it[53:216].mean()), float(it[216:].mean())]}
 
 
-def cpu_baseline(name, steps, workers):
-    """signals/s of the CPU restatement: `workers` processes (spawned) each
-    integrate `steps` of the 270 steps of one signal; throughput is scaled to
-    whole signals."""
-    total_steps = 270
-    # one thread per worker process: BLAS / OpenMP pools would oversubscribe the
-    # cores (the variables are read when a spawned worker loads numpy)
+def cpu_baseline(name, workers):
+    """signals/s of the CPU restatement: `workers` spawned processes, each
+    integrating one whole signal (set-up included); throughput = workers /
+    the slowest worker's time."""
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS"):
-        os.environ[var] = "1"
+        os.environ[var] = "1"    # one BLAS thread per process: a pool of them would oversubscribe the cores
     t0 = time.perf_counter()
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(workers) as pool:
-        res = pool.map(_cpu_sample_worker, [(name, steps, i) for i in range(workers)])
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = pool.map(_cpu_signal_worker, [(name, i) for i in range(workers)])
     wall = time.perf_counter() - t0
-    per_step = max(e / s for e, s in res)      # slowest worker's solve time per step
-    sig_per_s = workers / (per_step * total_steps)
-    return {"value": sig_per_s, "unit": "signals/s", "cores": workers, "kind": "port",
-            "sample": "%d of %d Crank-Nicolson steps of one %s signal per process (time of the solve loop, "
-                      "assembly excluded), %d process(es); wall %.1f s" % (steps, total_steps, name, workers, wall)}
+    per = max(r["setup_s"] + r["solve_s"] for r in res)
+    solve = max(r["solve_s"] for r in res)
+    it = np.mean([r["iterations"] for r in res], axis=0)
+    return {"value": workers / per, "unit": "signals/s", "cores": workers, "kind": "port",
+            "solve_only_value": workers / solve,
+            "sample": "%d whole signal(s) of the %s workload (all %d Crank-Nicolson steps, set-up included: mesh + "
+                      "assembly of the two-field forms), one per process, %d process(es) on %d core(s); slowest "
+                      "process %.1f s (solve %.1f s); BiCGSTAB iterations per step in the f=1 / f=0 / f=-1 regimes "
+                      "%.1f / %.1f / %.1f; wall %.1f s"
+                      % (workers, name, res[0]["steps"], workers, workers, per, solve, it[0], it[1], it[2], wall),
+            "normalized_signals": [r["normalized"] for r in res[:2]]}
 
 
-# ---------------------------------------------------------------- GPU leg ----
+# ---------------------------------------------------------------- GPU legs ---
+def _event_timer(stream, flush):
+    import torch
+
+    def timed(fn):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+    return timed
+
+
+def _signal_arrays(pkg, w, sel):
+    prof = w["profiles"]
+    int4 = [p.int4gb() for p in prof]
+    q = np.array([pkg.sequences.b_to_q(b, int4[pi]) for b, _, pi in sel])
+    g = np.array([gd for _, gd, _ in sel], np.float64)
+    g /= np.linalg.norm(g, axis=1, keepdims=True)
+    pidx = np.array([pi for _, _, pi in sel], np.int32)
+    return q, g, pidx
+
+
+def _context(pkg, w, local, stream):
+    ctx = pkg.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    rc = None if w["multiple"] else np.zeros(w["n_regions"], np.int32)
+    ctx.mesh_upload(w["xyz"], w["tets"], w["region"], w["n_regions"], rc)
+    ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
+    ctx.assemble()
+    fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in w["profiles"]])
+    ctx.set_schedule(np.array(fns), np.array(fos), w["dt"])
+    return ctx, np.array(fns), np.array(fos)
+
+
+def roofline_fp64(info, st, n_sig, peak, peak_src, traffic):
+    iters = st["total_iterations"] / n_sig
+    byts = alg_bytes_fp64(info["n_dofs"], info["nnz"], st["steps"], iters)
+    launch_ms = st["stepper_ms"] / n_sig
+    ach = byts / (launch_ms / 1e3) / 1e9
+    out = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+           "traffic": traffic.get("bytes_per_launch") if traffic else None,
+           "kernel": "k_step64 (persistent FP64 CN/COCG stepper, one launch per signal)",
+           "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src}
+    if traffic:
+        out["note"] = ("L2-resident: ncu counts %.0f MB of DRAM traffic per launch, %.3f%% of the %.0f GB of "
+                       "algorithmic bytes, so `achieved` counts L2-served bytes and `frac` is not an HBM "
+                       "fraction; the kernel is bound by the FP64 pipe (GB300 runs FP64 at a small fraction of "
+                       "FP32; ncu: FP64 pipe active 59%% of peak, profiles/k_step64_cfg2.md)"
+                       % (traffic["bytes_per_launch"] / 1e6, 100.0 * traffic["bytes_per_launch"] / byts, byts / 1e9))
+    else:
+        out["note"] = "no DRAM capture for this workload"
+    return out
+
+
 def gpu_run(args):
     import torch
     rank = int(os.environ.get("RANK", "0"))
@@ -197,34 +298,25 @@ def gpu_run(args):
     pkg = importlib.import_module(PKG)
     replicas = importlib.import_module(PKG + ".replicas")
     pkg._native.load(pkg.build())
-    w = pkg.meshgen.workload(args.workload)
-    prof = w["profiles"]
-    fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in prof])
-    fn, fo = np.array(fns), np.array(fos)
-    int4 = [p.int4gb() for p in prof]
-    sig = w["signals"]
-    q = np.array([pkg.sequences.b_to_q(b, int4[pi]) for b, _, pi in sig])
-    g = np.array([gd for _, gd, _ in sig], np.float64)
-    g /= np.linalg.norm(g, axis=1, keepdims=True)
-    pidx = np.array([pi for _, _, pi in sig], np.int32)
-    nr = w["n_regions"]
-    rc = None if w["multiple"] else np.zeros(nr, np.int32)
-    prec = pkg.PRECISION_MIXED if args.precision == "mixed" else pkg.PRECISION_FP64
-    rtol = args.rtol if args.rtol else (1e-12 if prec == pkg.PRECISION_FP64 else 1e-9)
-
+    w = pkg.meshgen.workload("cfg2")
+    # the whole job's signal list: b in {1000, 3000} x one direction per rank
+    # ((0,1,0) on one GPU, as the configuration states); each rank integrates
+    # its contiguous shard (replicas only: no data-path collective)
+    dirs = [(0.0, 1.0, 0.0)] if world == 1 else [tuple(d) for d in pkg.meshgen.fibonacci_directions(world)]
+    job = [(b, d, 0) for d in dirs for b in (1000.0, 3000.0)]
+    mine = replicas.shard(len(job), rank, world)
+    sel = [job[i] for i in mine]
+    q, g, pidx = _signal_arrays(pkg, w, sel)
+    n_sig = len(sel)
     stream = torch.cuda.current_stream()
-    ctx = pkg.Context(local)
-    ctx.set_stream(stream.cuda_stream)
-    ctx.mesh_upload(w["xyz"], w["tets"], w["region"], nr, rc)
-    ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
-    ctx.assemble()
-    ctx.set_schedule(fn, fo, w["dt"])
+    ctx, fn, fo = _context(pkg, w, local, stream)
     info = ctx.info()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 512 MB > L2
-    n_sig = len(sig)
+    peak, peak_src = peak_hbm()
+    traffic = load_json("profiles", "traffic.json") or {}
 
-    def timed(precision, tol, steps, warmup):
-        """W untimed + K timed solves of the whole batch; CUDA events on the
+    def timed_steps(precision, tol, steps, warmup):
+        """W untimed + K timed solves of the shard; CUDA events on the
         library's stream (torch's current stream), L2 flushed between steps."""
         for _ in range(warmup):
             ctx.solve(q, g, pidx, None, precision, tol, args.maxit)
@@ -248,68 +340,25 @@ def gpu_run(args):
         tot = replicas.max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), device="cuda")
         return tot, outs, clk.summary()
 
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
-    else:
-        peak, peak_src = 6800.0, "fallback"
-    l2_note = ("L2-resident: the working set fits the 129 MB L2 within a step, so achieved/HBM-peak counts "
-               "L2-served bytes" if info["nnz"] * 44 + info["n_dofs"] * n_sig * 400 < 100e6 else
-               "working set larger than L2")
-
-    def roofline(kind, st):
-        if kind == "fp64":
-            iters = st["total_iterations"] / n_sig
-            byts = alg_bytes_fp64(info["n_dofs"], info["nnz"], st["steps"], iters)
-            launch_ms = st["stepper_ms"] / n_sig
-            kern = "k_step64 (persistent FP64 CN/COCG stepper, one launch per signal)"
-        else:
-            launches = max(1, -(-n_sig // 256))
-            per = n_sig / launches
-            iters = st["total_iterations"] / n_sig                 # inner iterations per launch
-            sweeps = st["refinements"] / launches
-            byts = alg_bytes_mixed(info["n_dofs"], info["nnz"], per, st["steps"], iters, sweeps)
-            launch_ms = st["stepper_ms"] / launches
-            kern = "k_batched (persistent mixed-precision batched stepper, %d signal(s) per launch)" % per
-        ach = byts / (launch_ms / 1e3) / 1e9
-        tr = None
-        tpath = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tpath):
-            t = json.load(open(tpath)).get("%s:%s" % (args.workload, kind))
-            tr = t["bytes_per_launch"] if t else None
-        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": tr, "kernel": kern, "bytes_per_launch": byts, "launch_ms": launch_ms,
-                "peak_source": peak_src + " hbm_gbs (copy)", "note": l2_note}
-
-    prec_main = pkg.PRECISION_MIXED if args.precision == "mixed" else pkg.PRECISION_FP64
-    tol_main = args.rtol if args.rtol else (1e-9 if prec_main == pkg.PRECISION_MIXED else 1e-12)
-    total_ms, outs, clocks = timed(prec_main, tol_main, args.steps, args.warmup)
-    value = world * n_sig * args.steps / (total_ms / 1e3)
+    # ---- headline: plain FP64 path
+    total_ms, outs, clocks = timed_steps(pkg.PRECISION_FP64, 1e-12, args.steps, args.warmup)
+    value = len(job) * args.steps / (total_ms / 1e3)
     st = outs[-1]["stats"]
     norm = outs[-1]["signal"] / outs[-1]["S0"]
-    kind = "mixed" if prec_main == pkg.PRECISION_MIXED else "fp64"
-    roof = roofline(kind, st)
-    launches = st["kernel_launches"]
+    gathered = replicas.gather_signals(mine, norm, len(job), device="cuda")
+    roof = roofline_fp64(info, st, n_sig, peak, peak_src, traffic.get("cfg2:fp64"))
+    gold = golden_cfg2()
+    err_oracle = [abs(float(v) - gold[b]) / abs(gold[b]) for (b, _, _), v in zip(sel, norm)
+                  if tuple(dirs[0]) == (0.0, 1.0, 0.0) and b in gold] if rank == 0 else []
 
-    plain = None
-    if prec_main == pkg.PRECISION_MIXED and args.fp64_steps > 0:
-        t64, o64, c64 = timed(pkg.PRECISION_FP64, 1e-12, args.fp64_steps, max(1, min(args.warmup, 2)))
-        s64 = o64[-1]["stats"]
-        n64 = o64[-1]["signal"] / o64[-1]["S0"]
-        plain = {"value": world * n_sig * args.fp64_steps / (t64 / 1e3), "unit": "signals/s",
-                 "ms_per_step": t64 / args.fp64_steps, "steps": args.fp64_steps, "rtol": 1e-12,
-                 "normalized_signals": [float(v) for v in n64],
-                 "iterations_per_signal": s64["total_iterations"] / n_sig,
-                 "roofline": roofline("fp64", s64), "clocks": c64}
-        plain["mixed_over_plain"] = value / plain["value"]
-        plain["max_rel_err_mixed_vs_fp64"] = float(np.max(np.abs(norm - n64) / np.abs(n64)))
-
-    batched = batched_leg(args, pkg, stream, flush, peak, peak_src) if args.batched_signals > 0 else None
-    uneven = uneven_leg(args, pkg, stream, flush) if args.uneven_meshes > 0 else None
-    adjoint = adjoint_leg(args, pkg, stream, flush) if args.adjoint_signals > 0 else None
-
+    legs = {}
+    if world == 1 and args.mixed_steps > 0:
+        legs["mixed_cfg2"] = mixed_cfg2_leg(args, pkg, ctx, q, g, pidx, norm, total_ms / args.steps, gold, sel,
+                                            traffic.get("cfg2:mixed"), info, peak, peak_src, timed_steps)
     # end to end through the public C-ABI from host buffers
     e2e_ms = []
+    rc = None if w["multiple"] else np.zeros(w["n_regions"], np.int32)
+    nr = w["n_regions"]
     h2d = (w["xyz"].nbytes + w["tets"].astype(np.int32).nbytes + w["region"].astype(np.int32).nbytes
            + 8 * nr * (2 + nr) + fn.nbytes + fo.nbytes + q.nbytes + g.nbytes + pidx.nbytes)
     d2h = 8 * (n_sig + 1)
@@ -323,176 +372,200 @@ def gpu_run(args):
         c2.set_coefficients(w["D"], w["invT2"], w["kappa"])
         c2.assemble()
         c2.set_schedule(fn, fo, w["dt"])
-        o2 = c2.solve(q, g, pidx, None, prec_main, tol_main, args.maxit)
+        o2 = c2.solve(q, g, pidx, None, pkg.PRECISION_FP64, 1e-12, args.maxit)
         _ = float(o2["signal"][0])                          # result on the host
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         c2.close()
-    e2e_value = n_sig / (statistics.median(e2e_ms) / 1e3) * world if e2e_ms else None
+    e2e_ms_max = replicas.max_over_ranks(statistics.median(e2e_ms), device="cuda") if e2e_ms else None
+    e2e_value = len(job) / (e2e_ms_max / 1e3) if e2e_ms else None
+    ctx.close()
+
+    if world == 1:
+        stream_legs = (("batched", batched_leg, args.batched_signals), ("uneven", uneven_leg, args.uneven_meshes),
+                       ("adjoint", adjoint_leg, args.adjoint_signals))
+        for key, fnc, n in stream_legs:
+            if n > 0:
+                legs[key] = fnc(args, pkg, stream, flush, peak, peak_src, traffic)
 
     res = None
     if rank == 0:
-        cpu = cpu_baseline(args.workload, args.cpu_sample_steps, 1) if args.cpu_sample_steps > 0 else None
+        cpu = cpu_baseline("cfg2", 1) if args.cpu_signals > 0 else None
         res = {
-            "metric": "Bloch-Torrey signals/s on 1 GB300 at <=1e-6 rel err (%s)" % args.workload,
+            "metric": METRIC,
             "value": value, "unit": "signals/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64" if kind == "fp64" else "f32 (inner COCG) + double-float residuals",
+            "dtype": "f64",
             "data": "synthetic (seeded Kuhn box mesh and centroid markers; no dataset)",
-            "config": {"workload": args.workload + ": " + WORKLOADS.get(args.workload, ""),
-                       "signals_per_step": n_sig, "precision": kind, "rtol": tol_main,
+            "config": {"workload": "cfg2: " + WORKLOADS["cfg2"],
+                       "signals_per_step": len(job), "signals_per_gpu": n_sig, "precision": "fp64", "rtol": 1e-12,
                        "n_dofs": info["n_dofs"], "nnz": info["nnz"], "time_steps": st["steps"],
-                       "l2": "flushed between timed steps (512 MB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "normalized_signals": [float(v) for v in norm],
+                       "l2": "flushed between timed steps (512 MB write); the workload itself is L2-resident",
+                       "parallelism": "replicas, signal list sharded over ranks" if world > 1 else "single GPU"},
+            "normalized_signals": [float(v) for v in gathered[:, 0]] if gathered is not None else None,
+            "rel_err_vs_oracle": err_oracle,
+            "max_rel_err_vs_oracle": max(err_oracle) if err_oracle else None,
             "iterations_per_signal": st["total_iterations"] / n_sig,
             "roofline": roof,
-            "plain_fp64": plain,
-            "batched": batched,
-            "uneven": uneven,
-            "adjoint": adjoint,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "signals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
                     "what": "bt_create+bt_mesh_upload (device graph build)+bt_set_coefficients+bt_assemble+"
-                            "bt_set_schedule+bt_solve, host arrays in, signals out; median of %d" % len(e2e_ms)},
-            "gpu_launches": int(launches) * args.steps,
+                            "bt_set_schedule+bt_solve (FP64), host arrays in, signals out; median of %d"
+                            % len(e2e_ms)},
+            "gpu_launches": int(st["kernel_launches"]) * args.steps,
             "clocks": clocks,
         }
+        res.update(legs)
         print(json.dumps(res))
-    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return res
 
 
-def batched_leg(args, pkg, stream, flush, peak, peak_src):
-    """The batched form on the eight-cylinder 64^3 workload: the first
-    `batched_signals` of its 512 signals (directions x b-values, PGSE and
-    cos-OGSE) in one mixed-precision launch, against the FP64 path on two of the
-    same signals (one FP64 launch per signal).  L2 flushed before each timed
-    launch."""
-    import torch
-    w = pkg.meshgen.workload("cfg3")
-    prof = w["profiles"]
-    fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in prof])
-    int4 = [p.int4gb() for p in prof]
-    sig = w["signals"]
-    idx = np.linspace(0, len(sig) - 1, args.batched_signals).astype(int)
-    sel = [sig[i] for i in idx]
-    q = np.array([pkg.sequences.b_to_q(b, int4[pi]) for b, _, pi in sel])
-    g = np.array([gd for _, gd, _ in sel], np.float64)
-    g /= np.linalg.norm(g, axis=1, keepdims=True)
-    pidx = np.array([pi for _, _, pi in sel], np.int32)
-    ctx = pkg.Context(int(os.environ.get("LOCAL_RANK", "0")))
-    ctx.set_stream(stream.cuda_stream)
-    ctx.mesh_upload(w["xyz"], w["tets"], w["region"], w["n_regions"], None)
-    ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
-    ctx.assemble()
-    ctx.set_schedule(np.array(fns), np.array(fos), w["dt"])
-    info = ctx.info()
-
-    def timed(fn):
-        flush.zero_()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        out = fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1), out
-
-    ctx.solve(q, g, pidx, None, pkg.PRECISION_MIXED, 1e-9, args.maxit)          # warm-up (autotuner)
-    ms_mix, out = timed(lambda: ctx.solve(q, g, pidx, None, pkg.PRECISION_MIXED, 1e-9, args.maxit))
-    two = [0, len(q) - 1]
-    ms_64, o64 = timed(lambda: ctx.solve(q[two], g[two], pidx[two], None, pkg.PRECISION_FP64, 1e-12, args.maxit))
-    st = out["stats"]
+def mixed_cfg2_leg(args, pkg, ctx, q, g, pidx, n64, ms64, gold, sel, traffic, info, peak, peak_src, timed_steps):
+    """The batched mixed-precision path on the same 40^3 workload (2 signals in
+    one launch), its per-signal error against the oracle and the FP64 path."""
+    tot, outs, clk = timed_steps(pkg.PRECISION_MIXED, 1e-9, args.mixed_steps, 2)
+    st = outs[-1]["stats"]
+    nm = outs[-1]["signal"] / outs[-1]["S0"]
     n_sig = len(q)
     iters = st["total_iterations"] / n_sig
     byts = alg_bytes_mixed(info["n_dofs"], info["nnz"], n_sig, st["steps"], iters, st["refinements"])
-    ach = byts / (st["stepper_ms"] / 1e3) / 1e9
-    err = float(np.max(np.abs(out["signal"][two] - o64["signal"]) / np.abs(o64["signal"])))
+    launch_ms = st["stepper_ms"]
+    ach = byts / (launch_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "traffic": traffic.get("bytes_per_launch") if traffic else None,
+            "kernel": "k_batched (persistent mixed-precision stepper, %d signals per launch)" % n_sig,
+            "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src}
+    if traffic:
+        roof["note"] = ("L2-resident: ncu counts %.0f MB of DRAM traffic per launch, %.2f%% of the algorithmic "
+                        "bytes; `frac` counts L2-served bytes" % (traffic["bytes_per_launch"] / 1e6,
+                                                                  100.0 * traffic["bytes_per_launch"] / byts))
+    err_or = [abs(float(v) - gold[b]) / abs(gold[b]) for (b, _, _), v in zip(sel, nm) if b in gold]
+    value = n_sig * args.mixed_steps / (tot / 1e3)
+    return {"workload": "cfg2 (the headline's workload) on the mixed-precision path", "precision": "mixed",
+            "dtype": "f32 inner COCG + double-float (FP32 pair, ~44 bit) residual, refinement and state; FP64 signal "
+                     "sum (a deviation from FP64 residuals, chosen because GB300's FP64 issue rate is low)",
+            "rtol": 1e-9, "signals": n_sig, "value": value, "unit": "signals/s", "ms_per_step": tot / args.mixed_steps,
+            "steps": args.mixed_steps, "mixed_over_plain_fp64": value / (n_sig / (ms64 / 1e3)),
+            "rel_err_vs_oracle": err_or, "rel_err_vs_fp64": [float(abs(a - b) / abs(b)) for a, b in zip(nm, n64)],
+            "iterations_per_signal": iters, "refinements": st["refinements"], "roofline": roof, "clocks": clk}
+
+
+def batched_leg(args, pkg, stream, flush, peak, peak_src, traffic):
+    """All 512 signals of the eight-cylinder 64^3 workload on the mixed path
+    (two launches of 256), against the FP64 path on `fp64_sample` signals
+    spread over the 512, and the error of every signal against the FP64 values
+    of the committed fixture."""
+    w = pkg.meshgen.workload("cfg3")
+    sig = w["signals"][:args.batched_signals]
+    q, g, pidx = _signal_arrays(pkg, w, sig)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx, fn, fo = _context(pkg, w, local, stream)
+    info = ctx.info()
+    timed = _event_timer(stream, flush)
+    # warm-up: the autotuner's 3-step trials for this batch size, on a short schedule
+    ctx.set_schedule(fn[:, :4], fo[:, :4], w["dt"])
+    ctx.solve(q[:256], g[:256], pidx[:256], None, pkg.PRECISION_MIXED, 1e-9, args.maxit)
+    ctx.set_schedule(fn, fo, w["dt"])
+    ms_mix, out = timed(lambda: ctx.solve(q, g, pidx, None, pkg.PRECISION_MIXED, 1e-9, args.maxit))
+    n_sig = len(q)
+    nm = out["signal"] / out["S0"]
+    samp = np.unique(np.linspace(0, n_sig - 1, max(1, args.fp64_sample)).astype(int))
+    ms_64, o64 = timed(lambda: ctx.solve(q[samp], g[samp], pidx[samp], None, pkg.PRECISION_FP64, 1e-12, args.maxit))
+    n64 = o64["signal"] / o64["S0"]
+    err_live = np.abs(nm[samp] - n64) / np.abs(n64)
+    fx = load_json("tests", "golden", "gpu_fp64_cfg3_signals.json")
+    per_signal = None
+    if fx and len(fx.get("normalized", [])) >= n_sig:
+        ref = np.asarray(fx["normalized"][:n_sig])
+        per_signal = (np.abs(nm - ref) / np.abs(ref)).tolist()
+    st = out["stats"]
+    launches = -(-n_sig // 256)
+    per = n_sig / launches
+    iters = st["total_iterations"] / n_sig
+    byts = alg_bytes_mixed(info["n_dofs"], info["nnz"], per, st["steps"], iters, st["refinements"] / launches)
+    launch_ms = st["stepper_ms"] / launches
+    ach = byts / (launch_ms / 1e3) / 1e9
+    Rp = 2 * int(per)
+    wset = info["n_dofs"] * (Rp * 8 * 6 + (Rp // 2) * 8 * 7) + info["nnz"] * 44
+    tr = (traffic or {}).get("cfg3:mixed")
     v_mix = n_sig / (ms_mix / 1e3)
-    v_64 = len(two) / (ms_64 / 1e3)
+    v_64 = len(samp) / (ms_64 / 1e3)
     ctx.close()
-    return {"workload": "cfg3: " + WORKLOADS["cfg3"], "signals": n_sig, "n_dofs": info["n_dofs"], "nnz": info["nnz"],
+    return {"workload": "cfg3: " + WORKLOADS["cfg3"], "precision": "mixed", "signals": n_sig,
+            "launches": launches, "n_dofs": info["n_dofs"], "nnz": info["nnz"],
             "value": v_mix, "unit": "signals/s", "ms": ms_mix,
-            "plain_fp64_value": v_64, "plain_fp64_signals_timed": len(two),
-            "mixed_over_plain": v_mix / v_64, "max_rel_err_mixed_vs_fp64": err,
+            "plain_fp64_value": v_64, "plain_fp64_signals_timed": len(samp),
+            "mixed_over_plain": v_mix / v_64,
+            "max_rel_err_vs_fp64_live": float(err_live.max()),
+            "rel_err_vs_fp64_all_signals": per_signal,
+            "max_rel_err_vs_fp64_all_signals": max(per_signal) if per_signal else None,
+            "fp64_reference": ("tests/golden/gpu_fp64_cfg3_signals.json (FP64 path, rtol 1e-12, every signal) and "
+                               "%d signals re-run live" % len(samp)),
             "iterations_per_signal": iters, "refinements": st["refinements"],
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "bytes_per_launch": byts, "launch_ms": st["stepper_ms"],
-                         "peak_source": peak_src + " hbm_gbs (copy)",
-                         "note": "algorithmic bytes (bench.alg_bytes_mixed); working set larger than L2"}}
+                         "traffic": tr.get("bytes_per_launch") if tr else None,
+                         "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src,
+                         "note": "algorithmic bytes (bench.alg_bytes_mixed); working set %.1f GB, %.0fx the L2"
+                                 % (wset / 1e9, wset / L2_BYTES)}}
 
 
-def adjoint_leg(args, pkg, stream, flush):
+def adjoint_leg(args, pkg, stream, flush, peak, peak_src, traffic):
     """Gradients: the layered-sphere 48^3 workload (4 layers, per-layer D and T2,
-    per-interface kappa), the first `adjoint_signals` of its 120 signals spread
-    evenly; the batched mixed-precision adjoint (bt_adjoint_batch, one set of
-    launches) against the FP64 adjoint of one signal (bt_adjoint), and the
-    gradient error of that signal."""
-    import torch
+    per-interface kappa), `adjoint_signals` of its 120 signals spread evenly;
+    the batched mixed-precision adjoint (bt_adjoint_batch, one set of launches)
+    against the FP64 adjoint (bt_adjoint) of three of them."""
     w = pkg.meshgen.workload("cfg4")
-    prof = w["profiles"]
-    fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in prof])
     sig = w["signals"]
     idx = np.linspace(0, len(sig) - 1, args.adjoint_signals).astype(int)
-    sel = [sig[i] for i in idx]
-    q = np.array([pkg.sequences.b_to_q(b, prof[pi].int4gb()) for b, _, pi in sel])
-    g = np.array([gd for _, gd, _ in sel], np.float64)
-    g /= np.linalg.norm(g, axis=1, keepdims=True)
-    ctx = pkg.Context(int(os.environ.get("LOCAL_RANK", "0")))
-    ctx.set_stream(stream.cuda_stream)
-    ctx.mesh_upload(w["xyz"], w["tets"], w["region"], w["n_regions"], None)
-    ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
-    ctx.assemble()
-    ctx.set_schedule(np.array(fns), np.array(fos), w["dt"])
-
-    def timed(fn_):
-        flush.zero_()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        out = fn_()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1), out
-
+    q, g, _ = _signal_arrays(pkg, w, [sig[i] for i in idx])
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx, _, _ = _context(pkg, w, local, stream)
+    timed = _event_timer(stream, flush)
     ctx.solve(q, g, None, None, pkg.PRECISION_MIXED, 1e-9, args.maxit)          # warm-up (autotuner)
     ms_b, out = timed(lambda: ctx.adjoint_batch(q, g, rtol=1e-9, max_iterations=args.maxit))
-    ms_64, ref = timed(lambda: ctx.adjoint(q[0], g[0], rtol=1e-12, max_iterations=args.maxit))
-    err = {k: float(np.max(np.abs(out[k][0] - ref[k])) / np.max(np.abs(ref[k])))
-           for k in ("dD", "dinvT2", "dkappa")}
+    chk = sorted({0, len(q) // 2, len(q) - 1})
+    ms_64 = []
+    err = {"dD": 0.0, "dinvT2": 0.0, "dkappa": 0.0}
+    sig_err = 0.0
+    for k in chk:
+        m, ref = timed(lambda: ctx.adjoint(q[k], g[k], rtol=1e-12, max_iterations=args.maxit))
+        ms_64.append(m)
+        for key in err:
+            err[key] = max(err[key], float(np.max(np.abs(out[key][k] - ref[key])) / np.max(np.abs(ref[key]))))
+        sig_err = max(sig_err, float(abs(out["signal"][k] - ref["signal"]) / abs(ref["signal"])))
     info = ctx.info()
     ctx.close()
     n = len(q)
+    v64 = 1.0 / (statistics.mean(ms_64) / 1e3)
     return {"workload": "layered sphere 48^3 (4 regions, D/T2 per layer, kappa per interface), PGSE, "
                         "%d signals in one batched adjoint" % n,
             "n_dofs": info["n_dofs"], "signals": n,
             "batched_mixed": {"gradients_per_s": n / (ms_b / 1e3), "ms": ms_b,
                               "parameters_per_signal": "D x4, 1/T2 x4, kappa x3"},
-            "fp64_one_signal": {"gradients_per_s": 1.0 / (ms_64 / 1e3), "ms": ms_64},
-            "ratio": (n / ms_b) / (1.0 / ms_64),
-            "max_rel_err_vs_fp64_adjoint": err,
-            "signal_rel_err": float(abs(out["signal"][0] - ref["signal"]) / abs(ref["signal"]))}
+            "fp64_adjoint": {"gradients_per_s": v64, "ms_per_signal": statistics.mean(ms_64),
+                             "signals_checked": chk},
+            "ratio": (n / (ms_b / 1e3)) / v64,
+            "max_rel_err_vs_fp64_adjoint": err, "signal_rel_err": sig_err}
 
 
-def uneven_leg(args, pkg, stream, flush):
+def uneven_leg(args, pkg, stream, flush, peak, peak_src, traffic):
     """Several meshes of uneven size in one persistent launch (bt_solve_multi):
     `uneven_meshes` seeded boxes of 8^3 ... 24^3 Kuhn cubes of 1.5 um with
     random z-cylinders (D 3e-3 / 2e-3, kappa U[1e-5,1e-4]), 4 b-values along one
     direction each, PGSE; against one launch per mesh, and the largest mesh
     against the FP64 path."""
-    import torch
     meshes = pkg.meshgen.uneven_meshes(count=args.uneven_meshes, seed=0, nmin=8, nmax=24, cube=1.5)
     p = pkg.sequences.pgse(10600, 43100)
     fn, fo = pkg.sequences.profile_samples(p, 200.0)
     qs = [pkg.sequences.b_to_q(b, p.int4gb()) for b in (1000.0, 2000.0, 3000.0, 4000.0)]
     gs = [[0.36, 0.48, 0.8]] * 4
     ctxs = []
+    local = int(os.environ.get("LOCAL_RANK", "0"))
     for m in meshes:
-        c = pkg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+        c = pkg.Context(local)
         c.set_stream(stream.cuda_stream)
         c.mesh_upload(m["xyz"], m["tets"], m["region"], 2)
         c.set_coefficients(m["D"], None, m["kappa"])
@@ -500,17 +573,7 @@ def uneven_leg(args, pkg, stream, flush):
         c.set_schedule(fn, fo, 200.0)
         ctxs.append(c)
     n = len(ctxs)
-
-    def timed(fn_):
-        flush.zero_()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        out = fn_()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1), out
-
+    timed = _event_timer(stream, flush)
     pkg.solve_multi(ctxs, [qs] * n, [gs] * n, rtol=1e-9)                          # warm-up (tuning)
     ms_one, out = timed(lambda: pkg.solve_multi(ctxs, [qs] * n, [gs] * n, rtol=1e-9))
     for c in ctxs:
@@ -524,13 +587,13 @@ def uneven_leg(args, pkg, stream, flush):
     nsig = 4 * n
     return {"workload": "%d seeded cylinder boxes, 8^3..24^3 Kuhn cubes of 1.5 um (%d..%d dofs), 4 b-values each, "
                         "PGSE 10600/43100 us" % (n, min(dofs), max(dofs)),
-            "signals": nsig, "value": nsig / (ms_one / 1e3), "unit": "signals/s", "ms": ms_one,
+            "precision": "mixed", "signals": nsig, "value": nsig / (ms_one / 1e3), "unit": "signals/s", "ms": ms_one,
             "separate_launches_value": nsig / (ms_sep / 1e3), "one_launch_over_separate": ms_sep / ms_one,
             "max_rel_err_vs_fp64_largest_mesh": err}
 
 
 def batched_profile(args):
-    """One short launch for a profiler: the batched leg's 64 signals on the
+    """One short launch for a profiler: `profile_signals` signals of the
     eight-cylinder 64^3 workload, schedule cut to `batched_profile` steps inside
     the first gradient pulse, geometry fixed (lanes-per-row 32, two blocks per
     SM, interleaved rows) so that no autotuner trial runs first."""
@@ -540,13 +603,9 @@ def batched_profile(args):
     n = args.batched_profile
     fns, fos = zip(*[pkg.sequences.profile_samples(p, w["dt"]) for p in w["profiles"]])
     fn, fo = np.array(fns)[:, 20:20 + n], np.array(fos)[:, 20:20 + n]
-    int4 = [p.int4gb() for p in w["profiles"]]
     sig = w["signals"]
-    sel = [sig[i] for i in np.linspace(0, len(sig) - 1, args.batched_signals).astype(int)]
-    q = np.array([pkg.sequences.b_to_q(b, int4[pi]) for b, _, pi in sel])
-    g = np.array([gd for _, gd, _ in sel], np.float64)
-    g /= np.linalg.norm(g, axis=1, keepdims=True)
-    pidx = np.array([pi for _, _, pi in sel], np.int32)
+    sel = [sig[i] for i in np.linspace(0, len(sig) - 1, args.profile_signals).astype(int)]
+    q, g, pidx = _signal_arrays(pkg, w, sel)
     ctx = pkg.Context(0)
     ctx.mesh_upload(w["xyz"], w["tets"], w["region"], w["n_regions"], None)
     ctx.set_coefficients(w["D"], w["invT2"], w["kappa"])
@@ -565,18 +624,15 @@ def reference_run(args):
     if rank != 0:
         return
     workers = os.cpu_count() or 1
-    vals = []
-    for _ in range(args.warmup_ref):
-        pass
-    for _ in range(args.ref_steps):
-        vals.append(cpu_baseline(args.workload, args.cpu_sample_steps_ref, workers))
+    vals = [cpu_baseline("cfg2", workers) for _ in range(args.ref_steps)]
     v = statistics.median(x["value"] for x in vals)
-    out = {"metric": "Bloch-Torrey signals/s on 1 GB300 at <=1e-6 rel err (%s)" % args.workload,
+    out = {"metric": METRIC,
            "value": v, "unit": "signals/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
            "steps": args.ref_steps, "warmup": 0, "higher_is_better": True, "scaling": "weak",
            "impl": "reference", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": args.workload + ": " + WORKLOADS.get(args.workload, "")},
+           "config": {"workload": "cfg2: " + WORKLOADS["cfg2"]},
            "cpu_baseline": {"value": v, "unit": "signals/s", "cores": workers, "kind": "port",
+                            "solve_only_value": statistics.median(x["solve_only_value"] for x in vals),
                             "sample": vals[-1]["sample"]},
            "e2e": {"value": v, "unit": "signals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -588,27 +644,23 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 path (0: skip)")
-    ap.add_argument("--rtol", type=float, default=None)
-    ap.add_argument("--maxit", type=int, default=5000)
+    ap.add_argument("--maxit", type=int, default=20000)
+    ap.add_argument("--mixed-steps", type=int, default=5, help="timed steps of the mixed leg on 40^3 (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-sample-steps", type=int, default=8)
-    ap.add_argument("--cpu-sample-steps-ref", type=int, default=6)
+    ap.add_argument("--cpu-signals", type=int, default=1, help="whole-signal CPU baseline on one core (0: skip)")
     ap.add_argument("--batched-profile", type=int, default=0,
                     help="only one short batched launch of this many steps, for a profiler")
+    ap.add_argument("--profile-signals", type=int, default=64, help="signals of the --batched-profile launch")
+    ap.add_argument("--batched-signals", type=int, default=512,
+                    help="signals of the eight-cylinder 64^3 batched leg (0: skip)")
+    ap.add_argument("--fp64-sample", type=int, default=8, help="FP64 signals timed against the batched leg")
     ap.add_argument("--adjoint-signals", type=int, default=16,
                     help="signals of the batched-adjoint leg on the 48^3 layered sphere (0: skip)")
     ap.add_argument("--uneven-meshes", type=int, default=16,
                     help="meshes of the uneven multi-mesh leg (0: skip)")
-    ap.add_argument("--batched-signals", type=int, default=64,
-                    help="signals of the eight-cylinder 64^3 batched leg (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
-    args.warmup_e2e = 0
-    args.warmup_ref = 0
-    args.ref_steps = max(1, min(args.steps, 3))
+    args.ref_steps = max(1, min(args.steps, 2))
     if args.batched_profile > 0:
         batched_profile(args)
     elif args.impl == "reference":

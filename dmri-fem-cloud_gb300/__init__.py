@@ -11,7 +11,7 @@ geometries (``meshgen``) and the build recipe (``build``).
 
 from . import _native, sequences, meshgen, meshfiles  # noqa: F401
 from .api import (  # noqa: F401
-    Mesh, KrylovSolver, MRI_parameters, MyDomain, MRI_simulation, PostProcessing, simulate,
+    Mesh, KrylovSolver, MRI_parameters, MyDomain, MRI_simulation, PostProcessing, simulate, project_cell_values,
 )
 from ._native import Context, BtError, PRECISION_FP64, PRECISION_MIXED, solve_multi  # noqa: F401
 

@@ -112,6 +112,37 @@ class Mesh:
         return float(self.cell_edge_lengths().max(axis=1).max())
 
 
+def project_cell_values(mymesh, cell_values, rtol=1e-14):
+    """L2 projection of a per-cell (DG0) field onto P1: the vertex values x with
+    M x = b, M the P1 mass matrix of the whole mesh and b_i = sum over cells c
+    of v_c |c| / 4.  This is the reference's ``project(disc_ic, mydomain.V)``
+    that turns a per-compartment initial condition into the continuous
+    ``Dirac_Delta`` handed to ``MRI_simulation.solve``
+    (``DiscontinuousInitialCondition.ipynb``, cell 10).  Host-side set-up only
+    (Jacobi-CG on the consistent mass matrix, which is well conditioned).
+    Returns one value per vertex, for ``solve(..., ic=...)``."""
+    import scipy.sparse as sps
+    import scipy.sparse.linalg as spla
+    xyz, tets = mymesh.xyz, mymesh.tets.astype(np.int64)
+    v = np.asarray(cell_values, np.float64).reshape(len(tets))
+    E = xyz[tets[:, 1:]] - xyz[tets[:, :1]]
+    vol = np.abs(np.linalg.det(E)) / 6.0
+    loc = (vol / 20.0)[:, None, None] * (1.0 + np.eye(4))[None]
+    rr = np.broadcast_to(tets[:, :, None], loc.shape).ravel()
+    cc = np.broadcast_to(tets[:, None, :], loc.shape).ravel()
+    n_v = len(xyz)
+    M = sps.coo_matrix((loc.ravel(), (rr, cc)), shape=(n_v, n_v)).tocsr()
+    b = np.bincount(tets.ravel(), weights=np.repeat(v * vol / 4.0, 4), minlength=n_v)
+    d = M.diagonal()
+    if np.any(d <= 0.0):
+        raise ValueError("project_cell_values: a vertex belongs to no cell")
+    P = spla.LinearOperator(M.shape, matvec=lambda x: x / d, dtype=np.float64)
+    x, info = spla.cg(M, b, x0=b / (4.0 * d), rtol=rtol, atol=0.0, maxiter=1000, M=P)
+    if info != 0:
+        raise RuntimeError("project_cell_values: CG did not converge")
+    return x
+
+
 class KrylovSolver:
     """Stand-in for DOLFIN's ``KrylovSolver`` (``GCloudDmriSolver.py:219-222``).
 

@@ -1,32 +1,65 @@
-"""torch.autograd.Function over the engine's discrete adjoint.
+"""torch.autograd.Functions over the engine's discrete adjoints.
 
 ``BlochTorreySignal.apply(D, invT2, kappa, engine, q, gdir, sequence)`` returns
 the normalised signal S/S0 of one FP64 solve as a 0-d tensor; its backward
 returns dS/dD (per region), dS/d(1/T2) (per region) and dS/dkappa (per region
 pair, symmetric matrix), computed by ``bt_adjoint`` during the forward call
-(one forward sweep, one checkpointed backward sweep).  Tensors live on the
-host: they are the tissue parameters, not the field.
+(one forward sweep, one checkpointed backward sweep).
+
+``BlochTorreySignals.apply(D, invT2, kappa, engine, q[n], gdir[n, 3],
+sequence[n] or None)`` does the same for n signals at once through the batched
+mixed-precision adjoint (``bt_adjoint_batch``: the signals advance together,
+forward and backward): it returns the n normalised signals, and its backward
+contracts the incoming gradient with the n per-signal derivatives.
+
+The tissue parameters may be CPU or CUDA tensors of any floating dtype; they
+are read on the host (they are a handful of numbers, not the field) and the
+gradients are returned on the parameters' own device and dtype.
 """
 
 import numpy as np
 import torch
 
 
+def _host(t):
+    return t.detach().to("cpu", torch.float64).numpy()
+
+
 class BlochTorreySignal(torch.autograd.Function):
     @staticmethod
     def forward(ctx, D, invT2, kappa, engine, q, gdir, sequence=0):
-        Dn = D.detach().cpu().double().numpy()
-        Tn = invT2.detach().cpu().double().numpy()
-        Kn = kappa.detach().cpu().double().numpy()
-        engine.set_coefficients(Dn, Tn, Kn)
+        engine.set_coefficients(_host(D), _host(invT2), _host(kappa))
         engine.assemble()
         out = engine.adjoint(q, gdir, sequence)
         S0 = engine.info()["volume"]
+        ctx.like = [(x.device, x.dtype) for x in (D, invT2, kappa)]
         ctx.save_for_backward(torch.from_numpy(out["dD"] / S0), torch.from_numpy(out["dinvT2"] / S0),
                               torch.from_numpy(out["dkappa"] / S0))
-        return torch.tensor(out["signal"] / S0, dtype=torch.float64)
+        return torch.tensor(out["signal"] / S0, dtype=D.dtype, device=D.device)
 
     @staticmethod
     def backward(ctx, grad):
-        gD, gT, gK = ctx.saved_tensors
-        return grad * gD, grad * gT, grad * gK, None, None, None, None
+        g = float(grad.detach().to("cpu", torch.float64))
+        outs = [(g * t).to(dev, dt) for t, (dev, dt) in zip(ctx.saved_tensors, ctx.like)]
+        return outs[0], outs[1], outs[2], None, None, None, None
+
+
+class BlochTorreySignals(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, D, invT2, kappa, engine, q, gdir, sequence=None):
+        engine.set_coefficients(_host(D), _host(invT2), _host(kappa))
+        engine.assemble()
+        out = engine.adjoint_batch(np.asarray(q, np.float64), np.asarray(gdir, np.float64), sequence)
+        S0 = engine.info()["volume"]
+        ctx.like = [(x.device, x.dtype) for x in (D, invT2, kappa)]
+        ctx.save_for_backward(torch.from_numpy(out["dD"] / S0), torch.from_numpy(out["dinvT2"] / S0),
+                              torch.from_numpy(out["dkappa"] / S0))
+        return torch.from_numpy(out["signal"] / S0).to(D.device, D.dtype)
+
+    @staticmethod
+    def backward(ctx, grad):
+        g = grad.detach().to("cpu", torch.float64)          # [n]
+        gD, gT, gK = ctx.saved_tensors                      # [n, nr], [n, nr], [n, nr, nr]
+        outs = [torch.tensordot(g, t, dims=1) for t in (gD, gT, gK)]
+        outs = [t.to(dev, dt) for t, (dev, dt) in zip(outs, ctx.like)]
+        return outs[0], outs[1], outs[2], None, None, None, None

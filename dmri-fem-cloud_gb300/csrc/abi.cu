@@ -481,8 +481,17 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
         } else if (k == "mixed.extrapolate") {
             BT_REQUIRE(iv >= 0 && iv <= 2, BT_ERR_INVALID, "mixed.extrapolate must be 0, 1 or 2");
             ctx->opt_mixed_extrapolate = iv;
+        } else if (k == "mixed.inner_reductions") {
+            BT_REQUIRE(iv == 1 || iv == 2, BT_ERR_INVALID, "mixed.inner_reductions must be 1 or 2");
+            ctx->opt_mixed_inner = iv;
+            bt::reset_tuning_mixed(ctx);
         } else if (k == "fp64.extrapolate") {
             ctx->opt_fp64_extrapolate = iv ? 1 : 0;
+        } else if (k == "wait.limit_ns") {
+            BT_REQUIRE(value >= 1e4 && value <= 6e10, BT_ERR_INVALID, "wait.limit_ns must be in [1e4, 6e10]");
+            ctx->opt_wait_ns = (unsigned long long)value;
+        } else if (k == "test.stall_first_wait") {
+            ctx->opt_stall_first_wait = iv ? 1 : 0;
         } else {
             throw bt::Error(BT_ERR_INVALID, "bt_set_option: unknown key " + k);
         }

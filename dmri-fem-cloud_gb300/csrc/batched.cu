@@ -51,6 +51,7 @@ constexpr int kWarpsB = 8;
 constexpr int kThreadsB = kWarpsB * 32;
 constexpr int kMaxRhs = 512;
 constexpr int kNV = 4;  // values per RHS in one reduction
+constexpr int kNV1 = 9; // values per RHS in the reduction of the single-reduction COCG iteration
 
 struct MixArgs;
 
@@ -64,6 +65,7 @@ struct SolverMixed {
     DevBuf<double> w;         // per row signal weight
     DevBuf<int32_t> rcomp;
     DevBuf<float2> uh, ul, rh, rl, d0, d1, ri, z, p, q;  // [n][Rp]
+    DevBuf<float2> z1, w1, q1;   // [n][Rp]: second buffers of the single-reduction iteration
     DevBuf<float2> h0, h1, h2;   // per signal [n][Rp/2]: total corrections of the last three steps
     DevBuf<float2> partials, fin;   // double-float (hi, lo) sums
     DevBuf<double> sigpart;      // [warps][64][1+kMaxCompartments]
@@ -112,6 +114,11 @@ struct MixArgs {
     float4* z;
     float4* p;
     float4* q;
+    // second buffers of the single-reduction iteration (z, w~, q~ alternate between
+    // even and odd iterations: buffer 0 is z / ri / q, buffer 1 these)
+    float4* z1;
+    float4* w1;
+    float4* q1;
     float2* hist[3];      // per signal: u_{m+1} - u_m of steps m = s-2, s-1, s (rotating by s % 3)
     int32_t extrap;       // initial guess: 0 u_n, 1 linear, 2 quadratic extrapolation in time
     float2* partials;
@@ -155,6 +162,8 @@ struct MixArgs {
     int32_t save_every;
     float2* save_h;
     float2* save_l;
+    unsigned long long wait_ns;  // time limit of every grid-wide wait
+    int32_t stall;               // failure-detection hook: the first wait runs out (stalled_wait on bar[4])
 };
 
 // ------------------------------------------------------------ double-float ----
@@ -241,10 +250,10 @@ __device__ __forceinline__ void kadd(KF& a, float x) {
 }
 
 // -------------------------------------------------------------- reductions ----
-// Each lane holds compensated sums v[2][kNV] for its two slots.  Lane sums are
+// Each lane holds compensated sums v[2][NV] for its two slots.  Lane sums are
 // combined as double-float pairs (error-free TwoSum), never in FP64, which is
-// slow on this GPU.  On return out[][] holds the grid-wide sums rounded to
-// FP32, bitwise identical in every block.
+// slow on this GPU.  On return out[][] holds the grid-wide sums as double-float
+// (hi, lo) pairs, bitwise identical in every block.
 __device__ __forceinline__ float2 dfa(float2 a, float2 b) {  // (hi, lo) + (hi, lo)
     float s, e;
     two_sum(a.x, b.x, s, e);
@@ -253,16 +262,16 @@ __device__ __forceinline__ float2 dfa(float2 a, float2 b) {  // (hi, lo) + (hi, 
     return make_float2(h, e - (h - s));
 }
 
-template <int LPR>
-__device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV], const MixArgs& a, int chunk,
+template <int LPR, int NV>
+__device__ __forceinline__ bool reduce_rhs(KF (&v)[2][NV], float2 (&out)[2][NV], const MixArgs& a, int chunk,
                                            int r0, unsigned nb, unsigned bid, unsigned& gen, float2* smem) {
     constexpr int C = 2 * LPR;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    float2 d[2][kNV];
+    float2 d[2][NV];
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
-        for (int k = 0; k < kNV; ++k) {
+        for (int k = 0; k < NV; ++k) {
             const float h = v[j][k].s - v[j][k].c;   // Kahan: true sum = s - c
             d[j][k] = make_float2(h, (v[j][k].s - h) - v[j][k].c);
         }
@@ -272,7 +281,7 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) {
+            for (int k = 0; k < NV; ++k) {
                 const float2 t = make_float2(__shfl_xor_sync(0xffffffffu, d[j][k].x, o),
                                              __shfl_xor_sync(0xffffffffu, d[j][k].y, o));
                 d[j][k] = dfa(d[j][k], t);
@@ -282,20 +291,20 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) smem[(wib * C + lane * 2 + j) * kNV + k] = d[j][k];
+            for (int k = 0; k < NV; ++k) smem[(wib * C + lane * 2 + j) * NV + k] = d[j][k];
     }
     __syncthreads();
     const int nchunks = a.Rp / C;
     // block partial for every slot: sum over this block's warps of that chunk, in order
-    for (int t = threadIdx.x; t < a.Rp * kNV; t += blockDim.x) {
-        const int r = t / kNV, k = t % kNV;
+    for (int t = threadIdx.x; t < a.Rp * NV; t += blockDim.x) {
+        const int r = t / NV, k = t % NV;
         const int c = r / C, o = r % C;
         float2 s = make_float2(0.f, 0.f);
         for (int wb = 0; wb < kWarpsB; ++wb)
-            if ((int)((bid * kWarpsB + wb) % nchunks) == c) s = dfa(s, smem[(wb * C + o) * kNV + k]);
-        a.partials[(size_t)bid * a.Rp * kNV + t] = s;
+            if ((int)((bid * kWarpsB + wb) % nchunks) == c) s = dfa(s, smem[(wb * C + o) * NV + k]);
+        a.partials[(size_t)bid * a.Rp * NV + t] = s;
     }
-    const int V = a.Rp * kNV;
+    const int V = a.Rp * NV;
     if (a.reduce_mode == 1) {
         // every block sums all partials itself, in the same fixed order as the last
         // block of mode 0 (so the sums are bitwise those of mode 0): no block waits
@@ -316,7 +325,7 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
                 unsigned spins = 0;
                 while (ld_acquire_u64(ctr) < want) {
                     if (++spins > kBarrierMaxSpins || (spins & 255u) == 0u &&
-                        (globaltimer_ns() - t0 > kBarrierTimeoutNs || ld_relaxed_i32(a.status) != DEV_OK)) {
+                        (globaltimer_ns() - t0 > a.wait_ns || ld_relaxed_i32(a.status) != DEV_OK)) {
                         atomicCAS(a.status, DEV_OK, DEV_TIMEOUT);
                         ok = 0;
                         break;
@@ -353,9 +362,9 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) out[j][k] = smem[(r0 + j) * kNV + k].x + smem[(r0 + j) * kNV + k].y;
+            for (int k = 0; k < NV; ++k) out[j][k] = smem[(r0 + j) * NV + k];
     } else if (a.reduce_mode == 2) {
-        if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
+        if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return false;
         // stage 2: one warp per value; lane l adds blocks l, l+32, ... and the
         // warp combines the 32 lane sums in a fixed butterfly (lane 0's order)
         const int gw = bid * kWarpsB + wib;
@@ -376,13 +385,12 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
                 s = dfa(s, make_float2(__shfl_xor_sync(0xffffffffu, s.x, o), __shfl_xor_sync(0xffffffffu, s.y, o)));
             if (lane == 0) a.fin[t] = s;
         }
-        if (!grid_barrier(a.bar, nb, a.status, gen)) return false;
+        if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return false;
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) {
-                const float2 f = __ldcg(&a.fin[(r0 + j) * kNV + k]);
-                out[j][k] = f.x + f.y;
+            for (int k = 0; k < NV; ++k) {
+                out[j][k] = __ldcg(&a.fin[(r0 + j) * NV + k]);
             }
     } else {
         // one stage: the last block to arrive sums all partials (G lanes per value
@@ -441,7 +449,7 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
                 unsigned spins = 0;
                 while (ld_acquire_u32(&a.bar[1]) != target) {
                     if (++spins > kBarrierMaxSpins || (spins & 255u) == 0u &&
-                        (globaltimer_ns() - t0 > kBarrierTimeoutNs || ld_relaxed_i32(a.status) != DEV_OK)) {
+                        (globaltimer_ns() - t0 > a.wait_ns || ld_relaxed_i32(a.status) != DEV_OK)) {
                         atomicCAS(a.status, DEV_OK, DEV_TIMEOUT);
                         s_ok = 0;
                         break;
@@ -458,7 +466,7 @@ __device__ __forceinline__ bool reduce_rhs(KF (&v)[2][kNV], float (&out)[2][kNV]
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < kNV; ++k) out[j][k] = smem[(r0 + j) * kNV + k].x + smem[(r0 + j) * kNV + k].y;
+            for (int k = 0; k < NV; ++k) out[j][k] = smem[(r0 + j) * NV + k];
     }
     __syncthreads();
     return true;
@@ -484,17 +492,286 @@ __device__ __noinline__ double2 periodic_term(const MixArgs& a, int row, int r0,
     return make_double2((1.0 - a.theta_d) * bx, (1.0 - a.theta_d) * by);
 }
 
+// ------------------------------------------------- single-reduction COCG ----
+// The lane's two slots of a float4 are (x, y) and (z, w).
+__device__ __forceinline__ float2 slot_of(const float4 v, const int j) {
+    return j ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
+}
+__device__ __forceinline__ double2 dd2(const float2 hi, const float2 lo) {   // two double-float sums -> complex
+    return make_double2((double)hi.x + (double)hi.y, (double)lo.x + (double)lo.y);
+}
+
+// q~_{k-1} = w~_{k-1} + beta_{k-1} q~_{k-2} and z_k = z_{k-1} - alpha_{k-1} q~_{k-1} for
+// the lane's two slots.  Every row that gathers z_k of a neighbour forms it with
+// this function from the same stored values, and so does the neighbour's owner:
+// all of them get the same bits.
+__device__ __forceinline__ float4 next_z(const float4 z, const float4 w, const float4 q, const float2 (&al)[2],
+                                          const float2 (&be)[2], float4& qn) {
+    qn.x = fmaf(be[0].x, q.x, fmaf(-be[0].y, q.y, w.x));
+    qn.y = fmaf(be[0].x, q.y, fmaf(be[0].y, q.x, w.y));
+    qn.z = fmaf(be[1].x, q.z, fmaf(-be[1].y, q.w, w.z));
+    qn.w = fmaf(be[1].x, q.w, fmaf(be[1].y, q.z, w.w));
+    float4 zn;
+    zn.x = fmaf(-al[0].x, qn.x, fmaf(al[0].y, qn.y, z.x));
+    zn.y = fmaf(-al[0].x, qn.y, fmaf(-al[0].y, qn.x, z.y));
+    zn.z = fmaf(-al[1].x, qn.z, fmaf(al[1].y, qn.w, z.z));
+    zn.w = fmaf(-al[1].x, qn.w, fmaf(-al[1].y, qn.z, z.w));
+    return zn;
+}
+
+// Inner FP32 Jacobi-COCG with ONE grid-wide reduction per iteration.
+//
+// With D the Jacobi diagonal, the iteration keeps the scaled residual z = D^-1 r,
+// w~ = D^-1 A z, q~ = D^-1 q (q = A p), p and the correction d.  Iteration k
+// (k = 0, 1, ...; alpha_{k-1}, beta_{k-1} known, both 0 for k = 0) does, in one
+// pass over the rows:
+//     q~_{k-1} = w~_{k-1} + beta_{k-1} q~_{k-2}      (also for every neighbour)
+//     z_k      = z_{k-1} - alpha_{k-1} q~_{k-1}      (also for every neighbour)
+//     w_k      = A z_k                               (the SpMV)
+//     p_{k-1}  = z_{k-1} + beta_{k-1} p_{k-2},  d_k = d_{k-1} + alpha_{k-1} p_{k-1}
+// and the lane sums of rho_k = r_k^T z_k, |r_k|^2, delta_k = z_k^T w_k,
+// sigma_k = z_k^T q_{k-1} and mu_{k-1} = p_{k-1}^T q_{k-1} (r = D z, q = D q~).
+// Neighbours' z_k are formed from their stored z_{k-1}, w~_{k-1}, q~_{k-2} (the
+// three gathered vectors alternate between two buffers, so nobody overwrites
+// what another row still reads), hence no barrier is needed between the update
+// and the SpMV.  After the one reduction:
+//     beta_k = rho_k / rho_{k-1},
+//     mu_k   = p_k^T A p_k = delta_k + 2 beta_k sigma_k + beta_k^2 mu_{k-1}
+// (only A = A^T and q_{k-1} = A p_{k-1} are used, with mu_{k-1} summed directly,
+// so no recurrence error accumulates in mu), alpha_k = rho_k / mu_k; the scalars
+// are combined in FP64.  This is the Chronopoulos-Gear rearrangement of CG
+// (Chronopoulos & Gear, J. Comput. Appl. Math. 25, 1989) applied to COCG's
+// unconjugated forms, with the Jacobi scaling folded into the stored vectors.
+// Vector traffic per slot and iteration: z, w~, q~ (gathered), p, d read; z, w~,
+// q~, p, d written -- ten accesses, against twelve and two reductions for the
+// two-reduction form.  Activity, divergence and stagnation rules are the same.
+// Returns false when a reduction failed (the kernel must leave).
+template <int LPR>
+__device__ __forceinline__ bool inner_single(const MixArgs& a, MixArgs& b, const float eps, float (&rr2)[2],
+                                             const float (&rrs)[2], const float (&tolb2)[2], float (&rrmin)[2],
+                                             float (&rrmark)[2], int (&itmark)[2], bool (&act)[2], int& it,
+                                             bool& failed, const int step, const int sweep, const float (&cn)[2],
+                                             const float (&gx)[2], const float (&gy)[2], const float (&gz)[2],
+                                             const int dsel, const int g0, const int gend, const int gstride,
+                                             const int slot, const int r0, const int c4, const int Rp4,
+                                             const int chunk, const unsigned nb, const unsigned bid, unsigned& gen,
+                                             unsigned& flip, float2* const part0, float2* const part1,
+                                             float2* smem) {
+    constexpr int G = 32 / LPR;
+    constexpr bool kShared = (LPR >= 8);
+    const int lane = threadIdx.x & 31;
+    float2 al[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    float2 be[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    double2 rho_p[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    float4* const P = a.p;
+    float4* const Dv = a.dv[dsel];
+    const float4 f4z = make_float4(0.f, 0.f, 0.f, 0.f);
+    while (true) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            act[j] = (r0 + j < a.R) && rr2[j] > eps * eps * rrs[j] && rr2[j] > 0.09f * tolb2[j] &&
+                     rr2[j] <= a.growth2 * rrmin[j] && it - itmark[j] < 64;
+        if (!__syncthreads_or(act[0] || act[1])) break;
+        if (it >= a.maxit) {
+            if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+                if (bid == 0 && act[j]) {
+                    a.diag[0] = 1.0f; a.diag[1] = (float)step; a.diag[2] = (float)sweep; a.diag[3] = (float)it;
+                    a.diag[4] = rr2[j] / fmaxf(eps * eps * rrs[j], 1e-38f);
+                    a.diag[5] = (float)(r0 / 2);
+                }
+            failed = true;
+            break;
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            if (!act[j]) al[j] = be[j] = make_float2(0.f, 0.f);   // a finished slot keeps its d
+        // even iterations read buffer 0 and write buffer 1, odd ones the reverse
+        const bool odd = (it & 1) != 0;
+        const float4* const Zr = odd ? a.z1 : a.z;
+        const float4* const Wr = odd ? a.w1 : a.ri;
+        const float4* const Qr = odd ? a.q1 : a.q;
+        float4* const Zw = odd ? a.z : a.z1;
+        float4* const Ww = odd ? a.ri : a.w1;
+        float4* const Qw = odd ? a.q : a.q1;
+        KF v[2][kNV1];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < kNV1; ++k) v[j][k] = KF{0.0f, 0.0f};
+        const bool lane_active = act[0] || act[1];
+        for (int g = (kShared || lane_active) ? g0 : gend; g < gend; g += gstride) {
+            const int row_raw = g * G + slot;
+            if (!kShared && row_raw >= a.n) continue;
+            const bool row_ok = row_raw < a.n;
+            const int row = row_ok ? row_raw : a.n - 1;
+            const bool mine = row_ok && lane_active;
+            float2 sA[2], sx[2], sy[2], sz[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) sA[j] = sx[j] = sy[j] = sz[j] = make_float2(0.f, 0.f);
+            const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
+            auto acc_entry = [&](const float4 m, const float4 zz) {
+                const float2 zj[2] = {make_float2(zz.x, zz.y), make_float2(zz.z, zz.w)};
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    sA[j].x = fmaf(m.x, zj[j].x, sA[j].x); sA[j].y = fmaf(m.x, zj[j].y, sA[j].y);
+                    sx[j].x = fmaf(m.y, zj[j].x, sx[j].x); sx[j].y = fmaf(m.y, zj[j].y, sx[j].y);
+                    sy[j].x = fmaf(m.z, zj[j].x, sy[j].x); sy[j].y = fmaf(m.z, zj[j].y, sy[j].y);
+                    sz[j].x = fmaf(m.w, zj[j].x, sz[j].x); sz[j].y = fmaf(m.w, zj[j].y, sz[j].y);
+                }
+            };
+            if constexpr (kShared) {
+                // windows of 4 entries: lane gl < 4 of the row's group loads entry gl, the
+                // group shares column and values by shuffles, then 4 x 3 gathers go out
+                constexpr int W = 4;
+                const int gl = lane % LPR;
+                const int nn = e1 - e0;
+                const int nmax = __reduce_max_sync(0xffffffffu, nn);
+                for (int off = 0; off < nmax; off += W) {
+                    const bool ok = gl < W && off + gl < nn;
+                    const int my_c = ok ? a.col[e0 + off + gl] : row;
+                    const float4 my_m = ok ? a.mA[e0 + off + gl] : f4z;
+                    float4 zz[W], ww[W], qq[W];
+#pragma unroll
+                    for (int u = 0; u < W; ++u) {
+                        const int c = __shfl_sync(0xffffffffu, my_c, u, LPR);
+                        const size_t ni = (size_t)c * Rp4 + c4;
+                        zz[u] = mine ? __ldcg(&Zr[ni]) : f4z;
+                        ww[u] = mine ? __ldcg(&Wr[ni]) : f4z;
+                        qq[u] = mine ? __ldcg(&Qr[ni]) : f4z;
+                    }
+#pragma unroll
+                    for (int u = 0; u < W; ++u) {
+                        float4 m;
+                        m.x = __shfl_sync(0xffffffffu, my_m.x, u, LPR);
+                        m.y = __shfl_sync(0xffffffffu, my_m.y, u, LPR);
+                        m.z = __shfl_sync(0xffffffffu, my_m.z, u, LPR);
+                        m.w = __shfl_sync(0xffffffffu, my_m.w, u, LPR);
+                        float4 qn;
+                        acc_entry(m, next_z(zz[u], ww[u], qq[u], al, be, qn));
+                    }
+                }
+            } else {
+                // four neighbours (twelve gathers) in flight per lane; the tail of a
+                // row is predicated (a missing entry reads the own row times zero)
+                for (int e = e0; e < e1; e += 4) {
+                    int cc[4];
+                    float4 mm[4], zz[4], ww[4], qq[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const bool ok = e + u < e1;
+                        cc[u] = ok ? a.col[e + u] : row;
+                        mm[u] = ok ? a.mA[e + u] : f4z;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const size_t ni = (size_t)cc[u] * Rp4 + c4;
+                        zz[u] = __ldcg(&Zr[ni]);
+                        ww[u] = __ldcg(&Wr[ni]);
+                        qq[u] = __ldcg(&Qr[ni]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        float4 qn;
+                        acc_entry(mm[u], next_z(zz[u], ww[u], qq[u], al, be, qn));
+                    }
+                }
+            }
+            if (mine) {
+                const size_t vi = (size_t)row * Rp4 + c4;
+                const float4 zo = __ldcg(&Zr[vi]), wo = __ldcg(&Wr[vi]), qo = __ldcg(&Qr[vi]);
+                const float4 po = P[vi], dd = Dv[vi];
+                const float4 dgr = a.dg[row];
+                float4 qn;
+                const float4 zn = next_z(zo, wo, qo, al, be, qn);
+                float pn[4], dn[4], wt[4];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const float jr = gx[j] * sx[j].x + gy[j] * sy[j].x + gz[j] * sz[j].x;
+                    const float ji = gx[j] * sx[j].y + gy[j] * sy[j].y + gz[j] * sz[j].y;
+                    const float2 wv = make_float2(fmaf(-cn[j], ji, sA[j].x), fmaf(cn[j], jr, sA[j].y));   // w_k = A z_k
+                    const float2 Dg = make_float2(dgr.x, cn[j] * (gx[j] * dgr.y + gy[j] * dgr.z + gz[j] * dgr.w));
+                    const float2 wtj = cmulf(cinvf(Dg), wv);
+                    const float2 zj = slot_of(zn, j), qj = slot_of(qn, j);
+                    const float2 bp = cmulf(be[j], slot_of(po, j));
+                    const float2 zoj = slot_of(zo, j);
+                    const float2 pj = make_float2(zoj.x + bp.x, zoj.y + bp.y);            // p_{k-1}
+                    const float2 ap = cmulf(al[j], pj);
+                    const float2 dj = slot_of(dd, j);
+                    pn[2 * j] = pj.x;
+                    pn[2 * j + 1] = pj.y;
+                    dn[2 * j] = dj.x + ap.x;
+                    dn[2 * j + 1] = dj.y + ap.y;
+                    wt[2 * j] = wtj.x;
+                    wt[2 * j + 1] = wtj.y;
+                    const float2 rj = cmulf(Dg, zj);        // r_k
+                    const float2 qu = cmulf(Dg, qj);        // q_{k-1}
+                    const float2 rz = cmulf(rj, zj), zw = cmulf(zj, wv), zq = cmulf(zj, qu), pq = cmulf(pj, qu);
+                    kadd(v[j][0], rz.x);
+                    kadd(v[j][1], rz.y);
+                    kadd(v[j][2], rj.x * rj.x + rj.y * rj.y);
+                    kadd(v[j][3], zw.x);
+                    kadd(v[j][4], zw.y);
+                    kadd(v[j][5], zq.x);
+                    kadd(v[j][6], zq.y);
+                    kadd(v[j][7], pq.x);
+                    kadd(v[j][8], pq.y);
+                }
+                Zw[vi] = zn;
+                Ww[vi] = make_float4(wt[0], wt[1], wt[2], wt[3]);
+                Qw[vi] = qn;
+                P[vi] = make_float4(pn[0], pn[1], pn[2], pn[3]);
+                Dv[vi] = make_float4(dn[0], dn[1], dn[2], dn[3]);
+            }
+        }
+        float2 o[2][kNV1];
+        b.partials = (flip++ & 1u) ? part1 : part0;
+        if (!reduce_rhs<LPR, kNV1>(v, o, b, chunk, r0, nb, bid, gen, smem)) return false;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if (!act[j]) continue;
+            const double2 rho = dd2(o[j][0], o[j][1]);
+            const float nu = o[j][2].x + o[j][2].y;
+            const double2 delta = dd2(o[j][3], o[j][4]);
+            const double2 sigma = dd2(o[j][5], o[j][6]);
+            const double2 mud = dd2(o[j][7], o[j][8]);
+            const double rpn = rho_p[j].x * rho_p[j].x + rho_p[j].y * rho_p[j].y;
+            const double2 beta = (it == 0 || !(rpn > 0.0)) ? make_double2(0.0, 0.0) : cdiv(rho, rho_p[j]);
+            const double2 bs = cmul(beta, sigma), bbm = cmul(cmul(beta, beta), mud);
+            const double2 mu = make_double2(delta.x + 2.0 * bs.x + bbm.x, delta.y + 2.0 * bs.y + bbm.y);
+            const double mun = mu.x * mu.x + mu.y * mu.y, rhn = rho.x * rho.x + rho.y * rho.y;
+            const bool ok = mun > 0.0 && isfinite(mun) && rhn > 0.0 && isfinite(rhn);
+            const double2 alpha = ok ? cdiv(rho, mu) : make_double2(0.0, 0.0);
+            al[j] = make_float2((float)alpha.x, (float)alpha.y);
+            be[j] = ok ? make_float2((float)beta.x, (float)beta.y) : make_float2(0.f, 0.f);
+            rho_p[j] = rho;
+            rr2[j] = nu;
+            rrmin[j] = fminf(rrmin[j], nu);
+            if (nu < 0.25f * rrmark[j]) {
+                rrmark[j] = nu;
+                itmark[j] = it + 1;
+            }
+        }
+        ++it;
+    }
+    return true;
+}
+
 // ------------------------------------------------------------------ kernel ----
 // The stepper on one mesh, run by blocks bid = 0..nb-1 of a (sub-)grid whose
 // blocks are all co-resident.
 // kX: the optional paths (pseudo-periodic term, adjoint right-hand side w,
 // per-step state saves) are compiled only into the kX = true kernels, so the
 // plain stepper keeps the register allocation it has without them.
-template <int LPR, bool kX>
+// kS: the inner FP32 solve runs the single-reduction COCG iteration (one grid-wide
+// reduction per iteration, see below) instead of the two-reduction one.
+template <int LPR, bool kX, bool kS>
 __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bid, const unsigned nb) {
     constexpr int G = 32 / LPR;  // rows per warp-unit
     constexpr int C = 2 * LPR;   // RHS per warp-unit
-    __shared__ float2 smem[kWarpsB * 64 * kNV > kMaxRhs * kNV ? kWarpsB * 64 * kNV : kMaxRhs * kNV];
+    constexpr int NVM = kS ? kNV1 : kNV;   // widest reduction of this variant
+    __shared__ float2 smem[kWarpsB * 64 * NVM > kMaxRhs * NVM ? kWarpsB * 64 * NVM : kMaxRhs * NVM];
     const int lane = threadIdx.x & 31;
     const int gw = bid * kWarpsB + (threadIdx.x >> 5);
     const int total_warps = nb * kWarpsB;
@@ -519,6 +796,10 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
         gstride = total_warps / nchunks;
     }
     unsigned gen = 0;
+    if (a.stall) {   // bar[4] is never written: the wait runs out and the launch ends with DEV_TIMEOUT
+        stalled_wait(a.bar + 4, a.status, a.wait_ns);
+        return;
+    }
     // per-lane RHS parameters
     double qd[2];
     float gx[2], gy[2], gz[2];
@@ -533,13 +814,16 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
     }
     // partial buffers alternate between consecutive reductions (see reduce_rhs)
     float2* const part0 = a.partials;
-    float2* const part1 = a.partials + (size_t)nb * a.Rp * kNV;
+    float2* const part1 = a.partials + (size_t)nb * a.Rp * NVM;
     unsigned flip = 0;
     MixArgs b = a;
-#define BT_REDUCE(V, OUT)                                                     \
-    do {                                                                      \
-        b.partials = (flip++ & 1u) ? part1 : part0;                           \
-        if (!reduce_rhs<LPR>(V, OUT, b, chunk, r0, nb, bid, gen, smem)) return; \
+#define BT_REDUCE(V, OUT)                                                                  \
+    do {                                                                                   \
+        float2 o2_[2][kNV];                                                                \
+        b.partials = (flip++ & 1u) ? part1 : part0;                                        \
+        if (!reduce_rhs<LPR, kNV>(V, o2_, b, chunk, r0, nb, bid, gen, smem)) return;        \
+        for (int j_ = 0; j_ < 2; ++j_)                                                     \
+            for (int k_ = 0; k_ < kNV; ++k_) OUT[j_][k_] = o2_[j_][k_].x + o2_[j_][k_].y;  \
     } while (0)
 
     int dsel = 0;
@@ -695,7 +979,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
             const float2 z0 = make_float2(dinv.x * re.h, dinv.y * re.h);
             const float2 z1 = make_float2(dinv.x * im.h, dinv.y * im.h);
-            a.ri[vi] = make_float4(re.h, 0.f, im.h, 0.f);
+            a.ri[vi] = kS ? make_float4(0.f, 0.f, 0.f, 0.f) : make_float4(re.h, 0.f, im.h, 0.f);
             a.z[vi] = make_float4(z0.x, z0.y, z1.x, z1.y);
             a.p[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
             a.q[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -739,6 +1023,12 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             int itmark[2] = {0, 0};
             bool act[2];
             int it = 0;
+            if constexpr (kS) {
+                if (!inner_single<LPR>(a, b, eps, rr2, rrs, tolb2, rrmin, rrmark, itmark, act, it, failed, step, sweep,
+                                       cn, gx, gy, gz, dsel, g0, gend, gstride, slot, r0, c4, Rp4, chunk, nb, bid, gen,
+                                       flip, part0, part1, smem))
+                    return;
+            } else {
             while (true) {
                 // lane-local activity of its two RHS; the block-wide OR is the same in every
                 // block (rr2 / rrs are grid-identical sums).  __syncthreads_or has barrier
@@ -954,6 +1244,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 }
                 ++it;
             }
+            }   // kS
             it_total += it;
             if (failed) break;
             // ---- phase U: d = d_re-part + i d_im-part ; u += d ; r -= A d (double-float);
@@ -1024,7 +1315,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
                 const float2 z0 = make_float2(dinv.x * nr.h, dinv.y * nr.h);
                 const float2 z1 = make_float2(dinv.x * ni.h, dinv.y * ni.h);
-                a.ri[vi] = make_float4(nr.h, 0.f, ni.h, 0.f);
+                a.ri[vi] = kS ? make_float4(0.f, 0.f, 0.f, 0.f) : make_float4(nr.h, 0.f, ni.h, 0.f);
                 a.z[vi] = make_float4(z0.x, z0.y, z1.x, z1.y);
                 a.p[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
                 a.q[vi] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1113,7 +1404,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             for (int k = 0; k <= kMaxCompartments; ++k)
                 wp[((size_t)gw * C + lane * 2 + j) * (1 + kMaxCompartments) + k] = acc[j][k];
     }
-    if (!grid_barrier(a.bar, nb, a.status, gen)) return;
+    if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return;
     // grid thread t finishes (RHS r, value k): sum over warps of r's chunk in warp order
     const int gt = bid * blockDim.x + threadIdx.x;
     for (int t = gt; t < a.Rp * (1 + kMaxCompartments); t += nb * blockDim.x) {
@@ -1126,16 +1417,16 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
     }
 }
 
-template <int LPR, bool kX>
-__global__ void __maxnreg__(120) k_batched(MixArgs a) {
-    batched_body<LPR, kX>(a, blockIdx.x, gridDim.x);
+template <int LPR, bool kX, bool kS>
+__global__ void __maxnreg__(kS ? 128 : 120) k_batched(MixArgs a) {
+    batched_body<LPR, kX, kS>(a, blockIdx.x, gridDim.x);
 }
 
 // Several meshes in one cooperative launch: blocks first[m] .. first[m+1]-1 form
 // the sub-grid of mesh m, which runs its own stepper with its own barrier
 // counters and reductions; meshes never wait for one another.
-template <int LPR, bool kX>
-__global__ void __maxnreg__(120) k_batched_multi(const MixArgs* __restrict__ args, const int* __restrict__ first,
+template <int LPR, bool kX, bool kS>
+__global__ void __maxnreg__(kS ? 128 : 120) k_batched_multi(const MixArgs* __restrict__ args, const int* __restrict__ first,
                                                  int n_meshes) {
     __shared__ MixArgs s_a;
     __shared__ int s_m;
@@ -1147,7 +1438,7 @@ __global__ void __maxnreg__(120) k_batched_multi(const MixArgs* __restrict__ arg
     }
     __syncthreads();
     const int m = s_m;
-    batched_body<LPR, kX>(s_a, blockIdx.x - first[m], first[m + 1] - first[m]);
+    batched_body<LPR, kX, kS>(s_a, blockIdx.x - first[m], first[m + 1] - first[m]);
 }
 
 // Pack the double-float matrix copies and the row data once per assembly/theta/dt.
@@ -1201,34 +1492,39 @@ namespace {
 using KFn = void (*)(MixArgs);
 using KFnMulti = void (*)(const MixArgs*, const int*, int);
 
-template <bool kX>
+template <bool kX, bool kS>
 KFnMulti kernel_multi_lpr(int lpr) {
     switch (lpr) {
-        case 1: return k_batched_multi<1, kX>;
-        case 2: return k_batched_multi<2, kX>;
-        case 4: return k_batched_multi<4, kX>;
-        case 8: return k_batched_multi<8, kX>;
-        case 16: return k_batched_multi<16, kX>;
-        default: return k_batched_multi<32, kX>;
+        case 1: return k_batched_multi<1, kX, kS>;
+        case 2: return k_batched_multi<2, kX, kS>;
+        case 4: return k_batched_multi<4, kX, kS>;
+        case 8: return k_batched_multi<8, kX, kS>;
+        case 16: return k_batched_multi<16, kX, kS>;
+        default: return k_batched_multi<32, kX, kS>;
     }
 }
 
-template <bool kX>
+template <bool kX, bool kS>
 KFn kernel_lpr(int lpr) {
     switch (lpr) {
-        case 1: return k_batched<1, kX>;
-        case 2: return k_batched<2, kX>;
-        case 4: return k_batched<4, kX>;
-        case 8: return k_batched<8, kX>;
-        case 16: return k_batched<16, kX>;
-        default: return k_batched<32, kX>;
+        case 1: return k_batched<1, kX, kS>;
+        case 2: return k_batched<2, kX, kS>;
+        case 4: return k_batched<4, kX, kS>;
+        case 8: return k_batched<8, kX, kS>;
+        case 16: return k_batched<16, kX, kS>;
+        default: return k_batched<32, kX, kS>;
     }
 }
 
-KFn kernel_for(int lpr, bool extras) { return extras ? kernel_lpr<true>(lpr) : kernel_lpr<false>(lpr); }
+// The optional paths (extras) run the two-reduction inner iteration; the plain
+// stepper runs the single-reduction one when `single`.
+KFn kernel_for(int lpr, bool extras, bool single) {
+    return extras ? kernel_lpr<true, false>(lpr) : (single ? kernel_lpr<false, true>(lpr) : kernel_lpr<false, false>(lpr));
+}
 
-KFnMulti kernel_multi_for(int lpr, bool extras) {
-    return extras ? kernel_multi_lpr<true>(lpr) : kernel_multi_lpr<false>(lpr);
+KFnMulti kernel_multi_for(int lpr, bool extras, bool single) {
+    return extras ? kernel_multi_lpr<true, false>(lpr)
+                  : (single ? kernel_multi_lpr<false, true>(lpr) : kernel_multi_lpr<false, false>(lpr));
 }
 
 int ceil_pow2(int v) {
@@ -1284,7 +1580,7 @@ static int blocks_needed(const bt_ctx* ctx, int R, int lpr) {
 // mesh, for a (sub-)grid of nb blocks; nothing is launched.  n_steps may be
 // truncated for tuning.
 static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb, int blocked, int n_steps,
-                             double rtol, int maxit, const double* d_u0) {
+                             double rtol, int maxit, const double* d_u0, bool single) {
     Mesh& m = ctx->mesh;
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
@@ -1294,16 +1590,20 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     BT_REQUIRE(Rp >= R && Rp <= kMaxRhs && (Rp / (2 * lpr)) <= kWarpsB && (kWarpsB % (Rp / (2 * lpr))) == 0,
                BT_ERR_INVALID, "mixed stepper: invalid RHS padding");
     BT_REQUIRE(nb >= 1, BT_ERR_INVALID, "mixed stepper: empty grid");
-    // partials: two alternating float buffers [nb][Rp][kNV]
-    W.partials.alloc((size_t)2 * nb * Rp * kNV);
+    // partials: two alternating float buffers [nb][Rp][NV] for the widest reduction NV
+    const int nvm = single ? kNV1 : kNV;
+    W.partials.alloc((size_t)2 * nb * Rp * nvm);
     W.sigpart.alloc((size_t)nb * kWarpsB * 64 * (1 + kMaxCompartments));
-    W.fin.alloc((size_t)Rp * kNV);
+    W.fin.alloc((size_t)Rp * nvm);
     const size_t nv = (size_t)m.n_dofs * Rp;
     for (auto* v : {&W.d0, &W.d1, &W.ri, &W.z, &W.p, &W.q}) v->alloc(nv);        // per slot
+    if (single)
+        for (auto* v : {&W.z1, &W.w1, &W.q1}) v->alloc(nv);                     // second buffers of z, w~, q~
     for (auto* v : {&W.uh, &W.ul, &W.rh, &W.rl, &W.h0, &W.h1, &W.h2}) v->alloc(nv / 2);   // per signal
     for (auto* v : {&W.h0, &W.h1, &W.h2}) v->zero(s);
     W.sig.alloc((size_t)Rp * (1 + kMaxCompartments));
-    W.bar.alloc(4);   // [0], [1]: barrier / last-block arrival and release; [2..3]: 64-bit arrival counter
+    W.bar.alloc(6);   // [0], [1]: barrier / last-block arrival and release; [2..3]: 64-bit arrival counter;
+                      // [4]: never written (stalled_wait)
     W.status.alloc(1);
     W.diag.alloc(8);
     W.diag.zero(s);
@@ -1350,6 +1650,9 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     a.z = reinterpret_cast<float4*>(W.z.p);
     a.p = reinterpret_cast<float4*>(W.p.p);
     a.q = reinterpret_cast<float4*>(W.q.p);
+    a.z1 = single ? reinterpret_cast<float4*>(W.z1.p) : nullptr;
+    a.w1 = single ? reinterpret_cast<float4*>(W.w1.p) : nullptr;
+    a.q1 = single ? reinterpret_cast<float4*>(W.q1.p) : nullptr;
     a.hist[0] = W.h0.p;
     a.hist[1] = W.h1.p;
     a.hist[2] = W.h2.p;
@@ -1379,13 +1682,15 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
         // block summing them itself when that is at most 20 loads a thread (it saves
         // the publish / release / read-back round trips of the last-block form: 20 %
         // on the 20^3 box, 1-2 % on the 40^3 box; slower from ~10k partial values)
-        const size_t nvals = (size_t)nb * Rp * kNV;
+        const size_t nvals = (size_t)nb * Rp * nvm;
         a.reduce_mode = nvals > 12288 ? 2 : (ctx->opt_mixed_reduce >= 0 ? ctx->opt_mixed_reduce
                                                                          : (nvals <= 5120 ? 1 : 0));
     }
     a.blocked = blocked;
     a.iters = W.iters;
     a.sweeps = W.sweeps;
+    a.wait_ns = ctx->opt_wait_ns;
+    a.stall = ctx->opt_stall_first_wait;
     a.sig = W.sig;
     a.diag = W.diag;
     {
@@ -1441,13 +1746,15 @@ struct MixExtra {
 static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int blocked, int n_steps,
                           double rtol, int maxit, const double* d_u0, const MixExtra* ex = nullptr) {
     cudaStream_t s = ctx->stream;
-    KFn fn = kernel_for(lpr, ctx->per.on || (ex && (ex->rhs_w || ex->save_h)));
+    const bool extras = ctx->per.on || (ex && (ex->rhs_w || ex->save_h));
+    const bool single = !extras && ctx->opt_mixed_inner == 1;
+    KFn fn = kernel_for(lpr, extras, single);
     int occ = 0;
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
     BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
     const int per_sm = std::max(1, std::min(occ, per_sm_blocks));
     const int nb = std::max(1, std::min(per_sm * ctx->num_sms, blocks_needed(ctx, R, lpr)));
-    MixArgs a = prepare_batch(ctx, W, R, lpr, nb, blocked, n_steps, rtol, maxit, d_u0);
+    MixArgs a = prepare_batch(ctx, W, R, lpr, nb, blocked, n_steps, rtol, maxit, d_u0, single);
     if (ex) {
         const size_t vsz = (size_t)ctx->mesh.n_dofs * (a.Rp / 2);
         if (ex->zero_init) {
@@ -1713,7 +2020,8 @@ static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R
     cudaStream_t s = c0->stream;
     bool extras = false;
     for (int m = 0; m < nm; ++m) extras = extras || ctxs[m]->per.on;
-    KFnMulti fn = kernel_multi_for(lpr, extras);
+    const bool single = !extras && c0->opt_mixed_inner == 1;
+    KFnMulti fn = kernel_multi_for(lpr, extras, single);
     int occ = 0;
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreadsB, 0));
     BT_REQUIRE(occ >= 1, BT_ERR_CUDA, "mixed stepper kernel does not fit on an SM");
@@ -1726,7 +2034,7 @@ static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R
     for (int m = 0; m < nm; ++m) {
         SolverMixed& W = *ctxs[m]->smx;
         const int steps = std::min(n_steps_cap, ctxs[m]->sched.n_steps);
-        args[m] = prepare_batch(ctxs[m], W, R[m], lpr, nb[m], 0, steps, rtol, maxit, d_u0[m]);
+        args[m] = prepare_batch(ctxs[m], W, R[m], lpr, nb[m], 0, steps, rtol, maxit, d_u0[m], single);
         first[m + 1] = first[m] + nb[m];
     }
     SolverMixed& W0 = *c0->smx;

@@ -201,8 +201,13 @@ struct bt_ctx {
     int opt_mixed_extrapolate = 2;
     int opt_mixed_blocked = -1;
     int opt_mixed_reduce = -1;
-    double opt_mixed_growth2 = 1e8;   // divergence guard of a sweep (squared-norm growth over its minimum)   // grid sums of the mixed stepper: -1 by size, 0 last block, 1 every block
+    double opt_mixed_growth2 = 1e8;   // divergence guard of a sweep (squared-norm growth over its minimum)
     int opt_fp64_extrapolate = 1;
+    int opt_mixed_inner = 2;          // grid-wide reductions per inner COCG iteration: 1 or 2
+    // failure detection: time limit of every device-side wait, and a switch that
+    // makes the next solve's first wait run out (see stalled_wait)
+    unsigned long long opt_wait_ns = 2000000000ull;
+    int opt_stall_first_wait = 0;
 };
 
 namespace bt {
@@ -302,7 +307,7 @@ constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 constexpr unsigned kBarrierMaxSpins = 1u << 26;
 
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status,
-                                             unsigned& gen) {
+                                             unsigned& gen, unsigned long long limit_ns = kBarrierTimeoutNs) {
     __shared__ int s_ok;
     __threadfence();   // each thread's own stores are device-visible before its block arrives
     __syncthreads();
@@ -322,7 +327,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, in
                 unsigned spins = 0;
                 while (ld_acquire_u32(&bar[1]) != target) {
                     if (++spins > kBarrierMaxSpins || (spins & 255u) == 0u &&
-                        (globaltimer_ns() - t0 > kBarrierTimeoutNs || ld_relaxed_i32(status) != DEV_OK)) {
+                        (globaltimer_ns() - t0 > limit_ns || ld_relaxed_i32(status) != DEV_OK)) {
                         atomicCAS(status, DEV_OK, DEV_TIMEOUT);
                         ok = 0;
                         break;
@@ -337,6 +342,28 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, in
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// Failure-detection hook (option "test.stall_first_wait"): thread 0 of every
+// block waits for a word that nothing in the launch writes (never[0], zeroed
+// before the launch), so the wait runs out after limit_ns (or the poll limit),
+// records DEV_TIMEOUT in *status and every block leaves the kernel; the host
+// then reports BT_ERR_TIMEOUT and the context stays usable.  Returns false.
+__device__ __forceinline__ bool stalled_wait(const unsigned* never, int* status, unsigned long long limit_ns) {
+    if (threadIdx.x == 0) {
+        const unsigned long long t0 = globaltimer_ns();
+        unsigned spins = 0;
+        while (ld_acquire_u32(never) != 1u) {
+            if (++spins > kBarrierMaxSpins || (spins & 255u) == 0u &&
+                (globaltimer_ns() - t0 > limit_ns || ld_relaxed_i32(status) != DEV_OK)) {
+                atomicCAS(status, DEV_OK, DEV_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+        }
+    }
+    __syncthreads();
+    return false;
 }
 
 // Block-wide sum of NV doubles; the deterministic result is v[] of thread 0

@@ -14,7 +14,11 @@
 // not take the address of the array directly (the host-side symbol is only a
 // stand-in): the first call on each device, with that device current, looks up
 // its device address with cudaGetSymbolAddress and caches it.  That first call
-// should therefore happen before any stream capture begins.
+// should therefore happen before any stream capture begins.  The cache is keyed
+// by the device's current CUDA context as well (its unique id, read through the
+// driver entry point cuCtxGetId): after cudaDeviceReset the module is loaded
+// again, possibly at another address, and the next call looks the address up
+// again -- so after a reset, too, make one call before capturing.
 //
 // Limits and sharing: n must be at most kNoAllocMaxBlocks * kNoAllocPerBlock
 // elements (2,097,152 dofs); larger inputs are rejected.  Every call on a
@@ -67,6 +71,35 @@ k_signal_finish(const double* __restrict__ partials, int nblocks, double* __rest
 
 std::mutex g_noalloc_mutex;
 double* g_noalloc_addr[kMaxDevices] = {nullptr};
+unsigned long long g_noalloc_ctx[kMaxDevices] = {0};
+
+// Unique id of the calling thread's current CUDA context (0 when the driver
+// does not provide it).  Context ids are never reused within a process, so a
+// changed id means the cached symbol address may be stale.
+unsigned long long current_context_id() {
+    using GetCurrentFn = int (*)(void**);
+    using GetIdFn = int (*)(void*, unsigned long long*);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrentFn>(f1);
+            get_id = reinterpret_cast<GetIdFn>(f2);
+        }
+        looked_up = true;
+    }
+    if (!get_current || !get_id) return 0;
+    void* c = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&c) != 0 || !c || get_id(c, &id) != 0) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -82,10 +115,12 @@ extern "C" int bt_signal_noalloc(const double* d_weights, const double* d_u, int
     double* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_addr[dev]) {
+        const unsigned long long cid = current_context_id();
+        if (!g_noalloc_addr[dev] || g_noalloc_ctx[dev] != cid) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) return BT_ERR_CUDA;
             g_noalloc_addr[dev] = static_cast<double*>(p);
+            g_noalloc_ctx[dev] = current_context_id();   // the lookup may have created the context
         }
         scratch = g_noalloc_addr[dev];
     }

@@ -107,6 +107,8 @@ struct StepArgs {
     int32_t* iters;
     double* relres;
     double* out;
+    unsigned long long wait_ns;          // time limit of every grid-wide wait
+    int32_t stall;                       // failure-detection hook: the first wait runs out (stalled_wait)
 };
 
 // Grid-wide deterministic sum of NV doubles: block partials go to one of two
@@ -116,7 +118,7 @@ struct StepArgs {
 template <int NV>
 __device__ __forceinline__ bool reduce_all(double (&v)[NV], double* partials, unsigned nb, unsigned& flip,
                                            unsigned* bar, int* status, unsigned& gen, double* sm,
-                                           double* red) {
+                                           double* red, unsigned long long wait_ns) {
     block_sum<NV>(v, sm);
     double* P = partials + (size_t)(flip & 1u) * nb * kRed;
     ++flip;
@@ -124,7 +126,7 @@ __device__ __forceinline__ bool reduce_all(double (&v)[NV], double* partials, un
 #pragma unroll
         for (int k = 0; k < NV; ++k) P[blockIdx.x * kRed + k] = v[k];
     }
-    if (!grid_barrier(bar, nb, status, gen)) return false;
+    if (!grid_barrier(bar, nb, status, gen, wait_ns)) return false;
     if ((threadIdx.x >> 5) == 0) {
         const int lane = threadIdx.x & 31;
         double t[NV];
@@ -159,6 +161,10 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
     unsigned gen = 0, flip = 0;
     double2* U[3] = {a.u0, a.u1, a.u2};
     double2* x = U[1];
+    if (a.stall) {   // bar[2] is never written: the wait runs out and the launch ends with DEV_TIMEOUT
+        stalled_wait(a.bar + 2, a.status, a.wait_ns);
+        return;
+    }
 
     for (int step = 0; step < a.n_steps; ++step) {
         const double cn = a.cn[step], co = a.co[step];
@@ -230,7 +236,7 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
             acc[2] += rr.x * rr.x + rr.y * rr.y;
             acc[3] += b.x * b.x + b.y * b.y;
         }
-        if (!reduce_all<4>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+        if (!reduce_all<4>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
         double2 rho = make_double2(acc[0], acc[1]);
         double rr2 = acc[2];
         const double bb2 = acc[3];
@@ -286,7 +292,7 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 mu[0] += pq.x;
                 mu[1] += pq.y;
             }
-            if (!reduce_all<2>(mu, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+            if (!reduce_all<2>(mu, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
             const double2 muv = make_double2(mu[0], mu[1]);
             const double mun = muv.x * muv.x + muv.y * muv.y;
             if (!(mun > 0.0) || !isfinite(mun)) {
@@ -313,7 +319,7 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 acc3[1] += rz.y;
                 acc3[2] += ri.x * ri.x + ri.y * ri.y;
             }
-            if (!reduce_all<3>(acc3, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+            if (!reduce_all<3>(acc3, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
             const double2 rho_new = make_double2(acc3[0], acc3[1]);
             rr2 = acc3[2];
             ++it;
@@ -358,7 +364,7 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
                 if (k == c) acc[1 + k] += v;
         }
     }
-    if (!reduce_all<kRed>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red)) return;
+    if (!reduce_all<kRed>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
     if (blockIdx.x == 0 && threadIdx.x < kRed) a.out[threadIdx.x] = red[threadIdx.x];
 }
 
@@ -435,7 +441,7 @@ static void prepare_fp64(bt_ctx* ctx, Solver64& W) {
     W.dA.alloc(W.n_pad); W.dJ.alloc(W.n_pad); W.w.alloc(W.n_pad);
     W.rcomp.alloc(W.n_pad);
     for (auto* v : {&W.u[0], &W.u[1], &W.u[2], &W.r, &W.z, &W.p, &W.q, &W.dinv}) v->alloc(W.n_pad);
-    W.bar.alloc(2);
+    W.bar.alloc(3);   // [0] arrivals, [1] generation, [2] never written (stalled_wait)
     W.status.alloc(1);
     W.cn.alloc(S.n_steps); W.co.alloc(S.n_steps);
     W.relres.alloc(S.n_steps);
@@ -507,6 +513,8 @@ static float run_steps_fp64(bt_ctx* ctx, Solver64& W, const double* d_cn, const 
     a.save_every = save_every > 0 ? save_every : 1;
     a.n_pad = W.n_pad;
     a.iters = W.iters; a.relres = W.relres; a.out = W.out;
+    a.wait_ns = ctx->opt_wait_ns;
+    a.stall = ctx->opt_stall_first_wait;
     {
         const void* need_ptrs[] = {a.sl_ptr, a.sl_w, a.col, a.aj, a.bre, a.dA, a.dJ, a.w, a.rcomp, a.u0, a.u1,
                                    a.u2, a.r, a.z, a.p, a.q, a.dinv, a.partials, a.bar, a.status, a.cn, a.co,

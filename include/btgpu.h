@@ -256,7 +256,16 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *                           all partials itself, -1 by size (default; same bits either way)
  *   "mixed.extrapolate"     initial guess of each step: 2 = 3u_n - 3u_{n-1} + u_{n-2} (default),
  *                           1 = 2u_n - u_{n-1}, 0 = u_n
- *   "fp64.extrapolate"      1: initial guess 2 u_n - u_{n-1} (default), 0: u_n */
+ *   "mixed.inner_reductions" grid-wide reductions per inner COCG iteration: 1 (the
+ *                           single-reduction rearrangement) or 2 (default, the textbook form); the
+ *                           adjoint's and the pseudo-periodic launches always use 2
+ *   "fp64.extrapolate"      1: initial guess 2 u_n - u_{n-1} (default), 0: u_n
+ * Failure detection (every device-side wait of the persistent steppers is
+ * bounded; a wait that runs out ends the launch and the call returns
+ * BT_ERR_TIMEOUT, leaving the context usable):
+ *   "wait.limit_ns"         time limit of every grid-wide wait (default 2e9 = 2 s; 1e4 .. 6e10)
+ *   "test.stall_first_wait" 1: every later solve's first wait is on a word nothing writes, so it
+ *                           runs out after wait.limit_ns (exercises the timeout path); 0 (default) off */
 int bt_set_option(bt_ctx* ctx, const char* key, double value);
 
 /* Signal functional S = sum_i weights[i] * Re(u[i]) of a device-resident state,
@@ -269,7 +278,9 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value);
  * cuda_stream (NULL: the legacy default stream) of the current device.
  * Scratch is a static 8 KB device array: n <= 2097152, larger n returns
  * BT_ERR_INVALID.  The first call on each device looks up that array's device
- * address, so make it before any stream capture begins.  Calls share the
+ * address, so make it before any stream capture begins (the address is looked
+ * up again when the device's context changes, e.g. after cudaDeviceReset, so
+ * after a reset make one call before capturing, too).  Calls share the
  * scratch: calls that overlap on the GPU race and must be serialised.
  * Returns a status code only (no context, so no bt_last_error text). */
 int bt_signal_noalloc(const double* d_weights, const double* d_u, int64_t n, double* d_signal,

@@ -28,9 +28,12 @@ run.  The restatement follows the reference's forms line by line:
 Parity pins (see ``tests/test_oracle_pins.py``):
 
 * ``ConvergenceTest.ipynb:245,261-263,353,366-395,423`` -- BoxMesh [-2.5,2.5]^3
-  n=5 (216 vertices / 750 tets), D=2e-3, PGSE delta=1000 Delta=10000, dt=10,
-  b=1000, g=(0,0,1), MUMPS LU, loop ``while t < T``: normalised signal
-  8.440078e-01 (7 printed digits) and free signal exp(-bD)=1.353e-01.
+  with 16 cubes per axis (the printed hmin 5.413e-01 = sqrt(3)*5/16 identifies
+  the run; the n=5 in the cell source is a later edit), D=2e-3, PGSE
+  delta=1000 Delta=10000, dt=10, b=1000, g=(0,0,1), MUMPS LU, loop
+  ``while t < T``: normalised signal 8.440078e-01 and q, g, hmin to all printed
+  digits (``tests/golden/reference_kats.json``); the 216/750 counts of the
+  n=5 box pin the BoxMesh layout.
 * b = 0 gives a normalised signal of exactly 1 (``ExplicitImplementation.ipynb:437``).
 * q = 0 with uniform T2 gives ((1 - k/(2 T2)) / (1 + k/(2 T2)))^N exactly.
 * The literal two-field formulation and the duplicated-node complex

@@ -2,8 +2,9 @@
 
 Reads the reference notebooks as text (they are outputs of the reference's
 solve path run with DOLFIN 2019.1.0) and writes tests/golden/reference_kats.json.
-Run here, where the reference checkout exists:
-    python tests/golden/extract_reference_kats.py /root/reference
+Run where a checkout of the reference exists, giving its root as the argument
+or in the environment variable DMRI_REFERENCE:
+    python tests/golden/extract_reference_kats.py <reference root>
 """
 
 import json
@@ -47,4 +48,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DMRI_REFERENCE")
+    if not root or not os.path.isdir(root):
+        sys.exit("give the reference checkout's root as the argument or in DMRI_REFERENCE")
+    main(root)

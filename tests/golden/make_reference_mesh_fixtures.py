@@ -1,7 +1,8 @@
 """Golden fixtures on meshes shipped with the reference.
 
-Run from the repository root (needs the reference tree at /root/reference):
-    python tests/golden/make_reference_mesh_fixtures.py
+Run from the repository root, giving the reference checkout's root as the
+argument or in the environment variable DMRI_REFERENCE:
+    python tests/golden/make_reference_mesh_fixtures.py <reference root>
 Reads comri/meshes/cyl6_r_3E_6_vol.msh.zip and cyl12_r_3E_6_vol.msh.zip of the
 reference with meshfiles.read_msh (the gmsh 2.2 files the reference's
 GCloud/Preprocessing scripts use; single compartment: every physical tag is 0),
@@ -24,11 +25,11 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 
 pkg = importlib.import_module("dmri-fem-cloud_gb300")
-REF = "/root/reference/comri/meshes"
 NAMES = ["cyl6_r_3E_6_vol", "cyl12_r_3E_6_vol"]
 
 
-def main():
+def main(ref_root):
+    REF = os.path.join(ref_root, "comri", "meshes")
     arrays, cases = {}, []
     prof = oracle.PGSE(10600, 43100)
     for name in NAMES:
@@ -53,4 +54,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DMRI_REFERENCE")
+    if not root or not os.path.isdir(root):
+        sys.exit("give the reference checkout's root as the argument or in DMRI_REFERENCE")
+    main(root)

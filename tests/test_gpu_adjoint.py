@@ -158,3 +158,37 @@ def test_batched_mixed_adjoint_matches_fp64(pkg, lib):
                 err = np.max(np.abs(out[k][i] - ref[k]))
                 assert err <= 1e-5 * scale, (stride, i, k, err / scale)
     ctx.close()
+
+
+def test_batched_autograd_and_16_cubed_layers(pkg, lib):
+    """The batched adjoint on a 16^3 layered sphere (a finer mesh than the other
+    adjoint tests) against the FP64 adjoint of a spread of its signals, and the
+    batched torch.autograd.Function: its backward equals the contraction of the
+    incoming gradient with the per-signal FP64 derivatives, and gradients come
+    back on the parameters' device and dtype."""
+    import torch
+    from importlib import import_module
+    ag = import_module(pkg.__name__ + ".autograd")
+    xyz, tets, reg, D, invT2, kp = layered_case(pkg, n=16)
+    ctx, q = make(pkg, xyz, tets, reg, D, invT2, kp)
+    dirs = pkg.meshgen.fibonacci_directions(6)
+    qs = np.array([q * f for f in (0.6, 0.8, 1.0, 1.0, 1.2, 0.9)])
+    refs = [ctx.adjoint(qs[i], dirs[i], rtol=1e-13, max_iterations=20000) for i in range(6)]
+    dev = torch.device("cuda", 0)
+    Dt = torch.tensor(D, dtype=torch.float32, device=dev, requires_grad=True)
+    Tt = torch.tensor(invT2, dtype=torch.float64, requires_grad=True)
+    Kt = torch.tensor(kp, dtype=torch.float64, device=dev, requires_grad=True)
+    s = ag.BlochTorreySignals.apply(Dt, Tt, Kt, ctx, qs, dirs, None)
+    assert s.shape == (6,) and s.device == dev and s.dtype == torch.float32
+    wts = torch.linspace(0.5, 1.5, 6, dtype=torch.float32, device=dev)
+    (s * wts).sum().backward()
+    assert Dt.grad.device == dev and Dt.grad.dtype == torch.float32 and Tt.grad.device.type == "cpu"
+    S0 = ctx.info()["volume"]
+    w = wts.cpu().double().numpy()
+    for key, got in (("dD", Dt.grad), ("dinvT2", Tt.grad), ("dkappa", Kt.grad)):
+        ref = sum(w[i] * refs[i][key] for i in range(6)) / S0
+        scale = max(np.max(np.abs(refs[i][key])) for i in range(6)) / S0
+        assert np.max(np.abs(got.detach().cpu().double().numpy() - ref)) <= 1e-5 * scale * w.sum(), key
+    for i in range(6):
+        assert abs(float(s[i]) - refs[i]["signal"] / S0) <= 1e-6 * abs(refs[i]["signal"] / S0) + 1e-7
+    ctx.close()

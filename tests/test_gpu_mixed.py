@@ -86,3 +86,28 @@ def test_mixed_b0_is_one(pkg, lib):
     out = ctx.solve([0.0, 0.0, 0.0], [[1, 0, 0]] * 3, precision=pkg.PRECISION_MIXED, rtol=1e-9)
     assert np.all(np.abs(out["signal"] / out["S0"] - 1.0) < 1e-9)
     ctx.close()
+
+
+@pytest.mark.parametrize("nsig", [2, 40])
+def test_single_and_two_reduction_iterations_agree(pkg, lib, nsig):
+    """The single-reduction inner iteration (default) and the two-reduction one
+    ("mixed.inner_reductions" = 2) solve the same problem: both within the
+    mixed tolerance of the FP64 path, and both deterministic."""
+    w = pkg.meshgen.workload("cfg3", n=14)
+    ctx = ctx_for(pkg, w)
+    idx = np.linspace(0, len(w["signals"]) - 1, nsig).astype(int)
+    q, g, pidx = signals_of(pkg, w, idx)
+    fp64 = ctx.solve(q, g, pidx, precision=pkg.PRECISION_FP64, rtol=1e-12)["signal"]
+    got = {}
+    for mode in (1, 2):
+        ctx.set_option("mixed.inner_reductions", mode)
+        a = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-9)
+        b = ctx.solve(q, g, pidx, precision=pkg.PRECISION_MIXED, rtol=1e-9)
+        assert np.array_equal(a["signal"], b["signal"]), mode
+        rel = np.abs(a["signal"] - fp64) / np.abs(fp64)
+        assert rel.max() <= MIX_RTOL, (mode, rel.max())
+        got[mode] = a
+    # both forms do comparable work (inner iterations within a factor of 1.5)
+    it1, it2 = got[1]["stats"]["total_iterations"], got[2]["stats"]["total_iterations"]
+    assert 0.66 * it2 <= it1 <= 1.5 * it2, (it1, it2)
+    ctx.close()

@@ -129,3 +129,20 @@ def test_workloads_shapes(pkg):
     assert len(w4["signals"]) == 120 and set(np.unique(w4["region"])) <= {0, 1, 2, 3}
     d = pkg.meshgen.fibonacci_directions(64)
     assert np.allclose(np.linalg.norm(d, axis=1), 1.0)
+
+
+def test_projection_of_cell_values(pkg):
+    """P1 projection: constants are reproduced and M x = b holds."""
+    xyz, tets = pkg.meshgen.kuhn_box(-3, 3, 5)
+    m = pkg.Mesh(xyz, tets)
+    x = pkg.project_cell_values(m, np.full(len(tets), 2.5))
+    assert np.max(np.abs(x - 2.5)) < 1e-12
+    rng = np.random.default_rng(2)
+    v = rng.uniform(0.0, 1.0, len(tets))
+    x = pkg.project_cell_values(m, v)
+    sd = oracle.duplicated_system(xyz, tets, np.zeros(len(tets), np.int64), 3e-3)
+    M = sd["M"]                                # one compartment: dofs are vertices in order
+    assert np.array_equal(sd["vertex"], np.arange(len(xyz)))
+    vol, _, _ = oracle.element_geometry(xyz, tets)
+    b = np.bincount(tets.ravel(), weights=np.repeat(v * vol / 4.0, 4), minlength=len(xyz))
+    assert np.max(np.abs(M @ x - b)) <= 1e-12 * np.max(np.abs(b))

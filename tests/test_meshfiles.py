@@ -8,7 +8,10 @@ import zipfile
 import numpy as np
 import pytest
 
-REF_MESHES = "/root/reference/comri/meshes"
+# the reference checkout's root, when present (DMRI_REFERENCE); the tests on its
+# shipped meshes are skipped without it
+REF_MESHES = os.path.join(os.environ.get("DMRI_REFERENCE", ""), "comri", "meshes") \
+    if os.environ.get("DMRI_REFERENCE") else ""
 
 
 def tet_volumes(xyz, tets):
@@ -163,7 +166,8 @@ def test_markers_from_submeshes(pkg):
     assert np.array_equal(mk2 == 2, inside) and np.array_equal(ph2 == 0, inside) and np.all(ph2[~inside] == 1)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference tree not present")
+@pytest.mark.skipif(not REF_MESHES or not os.path.isdir(REF_MESHES),
+                    reason="reference checkout not given (DMRI_REFERENCE)")
 @pytest.mark.parametrize("name", ["cyl6_r_3E_6_vol.msh.zip", "undyAxon_Ax_1E_6_vol.msh.zip"])
 def test_reference_shipped_meshes(pkg, name):
     """The meshes shipped with the reference parse: every declared node is used,
