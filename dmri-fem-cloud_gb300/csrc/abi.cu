@@ -486,7 +486,8 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
             ctx->opt_mixed_inner = iv;
             bt::reset_tuning_mixed(ctx);
         } else if (k == "fp64.extrapolate") {
-            ctx->opt_fp64_extrapolate = iv ? 1 : 0;
+            BT_REQUIRE(iv >= 0 && iv <= 4, BT_ERR_INVALID, "fp64.extrapolate must be in [0, 4]");
+            ctx->opt_fp64_extrapolate = iv;
         } else if (k == "wait.limit_ns") {
             BT_REQUIRE(value >= 1e4 && value <= 6e10, BT_ERR_INVALID, "wait.limit_ns must be in [1e4, 6e10]");
             ctx->opt_wait_ns = (unsigned long long)value;
