@@ -13,7 +13,7 @@ from . import _native, sequences, meshgen, meshfiles  # noqa: F401
 from .api import (  # noqa: F401
     Mesh, KrylovSolver, MRI_parameters, MyDomain, MRI_simulation, PostProcessing, simulate, project_cell_values,
 )
-from ._native import Context, BtError, PRECISION_FP64, PRECISION_MIXED, solve_multi  # noqa: F401
+from ._native import Context, BtError, PRECISION_FP64, PRECISION_MIXED, solve_multi, adjoint_multi  # noqa: F401
 
 
 def build(force=False, verbose=False):

@@ -33,7 +33,8 @@ EXPORTS = [
     "bt_assemble", "bt_set_schedule", "bt_solve", "bt_get_csr", "bt_get_matrix",
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
     "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
-    "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info", "bt_adjoint_batch",
+    "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info", "bt_adjoint_batch", "bt_adjoint_multi",
+    "bt_set_kappa_mode",
 ]
 
 
@@ -96,6 +97,7 @@ def load(path=None):
         "bt_mesh_info": (C.c_int, [_P, C.POINTER(MeshInfo)]),
         "bt_set_coefficients": (C.c_int, [_P, _D, _D, _D]),
         "bt_set_cell_diffusion": (C.c_int, [_P, _D]),
+        "bt_set_kappa_mode": (C.c_int, [_P, C.c_int32]),
         "bt_set_cell_T2": (C.c_int, [_P, _D]),
         "bt_assemble": (C.c_int, [_P]),
         "bt_set_schedule": (C.c_int, [_P, _D, _D, C.c_int32, C.c_int32, C.c_double, C.c_double]),
@@ -120,6 +122,8 @@ def load(path=None):
         "bt_periodic_info": (C.c_int, [_P, C.POINTER(PeriodicInfo)]),
         "bt_adjoint_batch": (C.c_int, [_P, C.c_int32, _D, _D, _I32, C.c_double, C.c_int32, C.c_int32,
                                        _D, _D, _D, _D, C.POINTER(Stats)]),
+        "bt_adjoint_multi": (C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _D, _I32, C.c_double, C.c_int32,
+                                       C.c_int32, _D, _D, _D, _D, C.POINTER(Stats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -204,6 +208,11 @@ class Context:
                 kp = np.full((self.n_regions, self.n_regions), float(kp))
             kp = np.ascontiguousarray(kp.reshape(self.n_regions, self.n_regions))
         self._check(self.lib.bt_set_coefficients(self.h, _dp(D), _dp(iT2), _dp(kp)))
+
+    def set_kappa_mode(self, mode):
+        """'facet' (one permeability per interface facet, the default) or 'cr'
+        (the Crouzeix-Raviart permeability field); takes effect at assemble()."""
+        self._check(self.lib.bt_set_kappa_mode(self.h, {"facet": 0, "cr": 1}[mode]))
 
     def set_cell_diffusion(self, D_cell6):
         arr = None if D_cell6 is None else np.ascontiguousarray(D_cell6, dtype=np.float64)
@@ -371,3 +380,42 @@ def solve_multi(contexts, q, gdir, sequence=None, rtol=1e-9, max_iterations=5000
                                           int(max_iterations), _dp(sig), _dp(S0), C.byref(st)))
     cuts = np.cumsum(nsig)[:-1]
     return {"signal": np.split(sig, cuts), "S0": S0, "stats": st.as_dict()}
+
+
+def adjoint_multi(contexts, q, gdir, sequence=None, rtol=1e-9, max_iterations=20000, stride=0):
+    """The batched mixed-precision adjoint of several meshes in one call.
+
+    ``contexts[m]`` holds mesh m (uploaded, assembled, with a schedule);
+    ``q[m]``, ``gdir[m]`` (and ``sequence[m]``) are that mesh's signals.  Returns
+    per mesh the signals and the unnormalised gradients: {"signal": [n_m],
+    "dD": [n_m x nr_m], "dinvT2": [n_m x nr_m], "dkappa": [n_m x nr_m x nr_m]}
+    lists, and the stats."""
+    nm = len(contexts)
+    qs = [np.atleast_1d(np.asarray(x, np.float64)) for x in q]
+    if len(qs) != nm or len(gdir) != nm:
+        raise ValueError("one q list and one gdir list per context")
+    nsig = np.ascontiguousarray([len(x) for x in qs], np.int32)
+    qa = np.ascontiguousarray(np.concatenate(qs))
+    ga = np.ascontiguousarray(np.concatenate([np.asarray(g, np.float64).reshape(len(x), 3)
+                                              for g, x in zip(gdir, qs)]))
+    sa = None if sequence is None else np.ascontiguousarray(
+        np.concatenate([np.asarray(s_, np.int32).reshape(len(x)) for s_, x in zip(sequence, qs)]))
+    nrs = [c.n_regions for c in contexts]
+    nD = int(sum(n * r for n, r in zip(nsig, nrs)))
+    nK = int(sum(n * r * r for n, r in zip(nsig, nrs)))
+    handles = (_P * nm)(*[c.h for c in contexts])
+    sig, dD, dT, dK = np.zeros(len(qa)), np.zeros(nD), np.zeros(nD), np.zeros(nK)
+    st = Stats()
+    lib = contexts[0].lib
+    contexts[0]._check(lib.bt_adjoint_multi(handles, nm, _ip(nsig), _dp(qa), _dp(ga), _ip(sa), float(rtol),
+                                            int(max_iterations), int(stride), _dp(sig), _dp(dD), _dp(dT), _dp(dK),
+                                            C.byref(st)))
+    out = {"signal": [], "dD": [], "dinvT2": [], "dkappa": [], "stats": st.as_dict()}
+    a = b = c = 0
+    for n, r in zip(nsig, nrs):
+        out["signal"].append(sig[a:a + n])
+        out["dD"].append(dD[b:b + n * r].reshape(n, r))
+        out["dinvT2"].append(dT[b:b + n * r].reshape(n, r))
+        out["dkappa"].append(dK[c:c + n * r * r].reshape(n, r, r))
+        a, b, c = a + n, b + n * r, c + n * r * r
+    return out

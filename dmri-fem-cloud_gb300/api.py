@@ -262,7 +262,9 @@ class MyDomain:
 
     ``phase`` (per cell, 0/1) or ``mymesh.markers`` select the compartments;
     ``kappa`` is a scalar or an (n_regions, n_regions) array (per-interface
-    permeability); ``D`` is a scalar, a per-region array, or a per-cell tensor
+    permeability), constant on each interface facet (``kappa_mode = "facet"``)
+    or, with ``kappa_mode = "cr"``, the reference's Crouzeix-Raviart permeability
+    field (``MultilayeredDiskVariablePermeability.ipynb:480-502``); ``D`` is a scalar, a per-region array, or a per-cell tensor
     set through :meth:`ImposeDiffusionTensor`.
     """
 
@@ -284,6 +286,7 @@ class MyDomain:
         self.IsDomainPeriodic = False
         self.IsDomainMultiple = False
         self.kappa = 0.0
+        self.kappa_mode = "facet"   # or "cr": the reference's Crouzeix-Raviart permeability field
         self.D = None
         self._D_cell = None
         self.device = 0
@@ -345,7 +348,7 @@ class MyDomain:
             kp = np.full((nr, nr), float(kp))
         Dr = np.broadcast_to(np.asarray(3e-3 if isinstance(D, str) else D, np.float64), (nr,)).copy()
         key = (Dr.tobytes(), iT2.tobytes(), kp.tobytes(), None if self._D_cell is None else id(self._D_cell),
-               None if iT2_cell is None else iT2_cell.tobytes())
+               None if iT2_cell is None else iT2_cell.tobytes(), self.kappa_mode)
         if self._ctx is None:
             self._ctx = _native.Context(self.device)
             self._ctx.mesh_upload(self.mymesh.xyz, self.mymesh.tets, reg, nr, rc)
@@ -361,6 +364,7 @@ class MyDomain:
             self._ctx.set_coefficients(Dr, iT2, kp)
             self._ctx.set_cell_diffusion(self._D_cell)
             self._ctx.set_cell_T2(iT2_cell)
+            self._ctx.set_kappa_mode(self.kappa_mode)
             self._ctx.assemble()
             self._state = key
         return self._ctx

@@ -174,6 +174,17 @@ int bt_set_coefficients(bt_ctx* ctx, const double* D_region, const double* invT2
     });
 }
 
+int bt_set_kappa_mode(bt_ctx* ctx, int32_t mode) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built, BT_ERR_STATE, "bt_set_kappa_mode: no mesh");
+        BT_REQUIRE(mode == BT_KAPPA_FACET || mode == BT_KAPPA_CR, BT_ERR_INVALID,
+                   "bt_set_kappa_mode: mode must be BT_KAPPA_FACET or BT_KAPPA_CR");
+        ctx->coeffs.kappa_cr = (mode == BT_KAPPA_CR);
+        ctx->mat.done = false;
+    });
+}
+
 int bt_set_cell_diffusion(bt_ctx* ctx, const double* D_cell) {
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
@@ -443,6 +454,49 @@ int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const doub
     });
 }
 
+int bt_adjoint_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_signals, const double* q,
+                     const double* gdir, const int32_t* sequence, double rtol, int32_t max_iterations,
+                     int32_t checkpoint_stride, double* signal_out, double* dS_dD, double* dS_dinvT2,
+                     double* dS_dkappa, bt_stats* stats) {
+    if (!contexts || n_meshes < 1 || !contexts[0]) return BT_ERR_INVALID;
+    bt_ctx* c0 = contexts[0];
+    return guarded(c0, [&] {
+        BT_REQUIRE(n_meshes <= 64 && n_signals && q && gdir && signal_out, BT_ERR_INVALID,
+                   "bt_adjoint_multi: bad arguments (at most 64 meshes)");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_adjoint_multi: rtol must be > 0 and max_iterations >= 1");
+        int64_t total = 0;
+        for (int32_t m = 0; m < n_meshes; ++m) {
+            bt_ctx* c = contexts[m];
+            BT_REQUIRE(c != nullptr, BT_ERR_INVALID, "bt_adjoint_multi: null context");
+            for (int32_t j = 0; j < m; ++j)
+                BT_REQUIRE(contexts[j] != c, BT_ERR_INVALID, "bt_adjoint_multi: a context is listed twice");
+            BT_REQUIRE(c->device == c0->device, BT_ERR_INVALID, "bt_adjoint_multi: contexts on different devices");
+            BT_REQUIRE(c->mesh.built && c->mat.done && c->sched.set, BT_ERR_STATE,
+                       "bt_adjoint_multi: every mesh needs bt_assemble and bt_set_schedule");
+            BT_REQUIRE(n_signals[m] >= 1 && n_signals[m] <= 256, BT_ERR_INVALID,
+                       "bt_adjoint_multi: 1..256 signals per mesh");
+            total += n_signals[m];
+        }
+        for (int64_t i = 0; i < total; ++i) {
+            BT_REQUIRE(std::isfinite(q[i]) && std::isfinite(gdir[3 * i]) && std::isfinite(gdir[3 * i + 1]) &&
+                           std::isfinite(gdir[3 * i + 2]),
+                       BT_ERR_INVALID, "bt_adjoint_multi: q and gradient directions must be finite");
+            if (sequence) {
+                int64_t acc = 0;
+                int32_t m = 0;
+                while (acc + n_signals[m] <= i) acc += n_signals[m++];
+                BT_REQUIRE(sequence[i] >= 0 && sequence[i] < contexts[m]->sched.n_seq, BT_ERR_INVALID,
+                           "bt_adjoint_multi: sequence index out of range");
+            }
+        }
+        use_device(c0);
+        for (int32_t m = 0; m < n_meshes; ++m) contexts[m]->last_precision = -1;
+        bt::adjoint_mixed_multi(contexts, n_meshes, n_signals, q, gdir, sequence, rtol, max_iterations,
+                                checkpoint_stride, signal_out, dS_dD, dS_dinvT2, dS_dkappa, stats);
+    });
+}
+
 int bt_set_option(bt_ctx* ctx, const char* key, double value) {
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
@@ -479,7 +533,7 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
             BT_REQUIRE(value >= 1.0, BT_ERR_INVALID, "mixed.divergence must be >= 1");
             ctx->opt_mixed_growth2 = value * value;
         } else if (k == "mixed.extrapolate") {
-            BT_REQUIRE(iv >= 0 && iv <= 2, BT_ERR_INVALID, "mixed.extrapolate must be 0, 1 or 2");
+            BT_REQUIRE(iv >= 0 && iv <= 4, BT_ERR_INVALID, "mixed.extrapolate must be in [0, 4]");
             ctx->opt_mixed_extrapolate = iv;
         } else if (k == "mixed.inner_reductions") {
             BT_REQUIRE(iv == 1 || iv == 2, BT_ERR_INVALID, "mixed.inner_reductions must be 1 or 2");

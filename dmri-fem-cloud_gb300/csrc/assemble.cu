@@ -10,6 +10,14 @@
 //   Jk_ij = V/60 (2 x_i + S) (i=j), V/120 (x_i + x_j + S) (i!=j),  S = sum x
 //   R     = kappa int_F [u][v] on interface facets: +B on (a,a),(b,b), -B on
 //           (a,b),(b,a), B_ij = kappa A/12 (1 + d_ij)   (icondition_wBC)
+//           With a Crouzeix-Raviart kappa (the per-interface permeability of
+//           MultilayeredDiskVariablePermeability.ipynb:480-502: the CR dof of a
+//           facet is the region pair's value where the regions differ, else 0),
+//           kappa is linear on each side of the facet, with vertex values
+//           sum_g kappa_g - 3 kappa_opposite(v) (the P1 function whose face
+//           centroids carry the four dofs), and avg() takes the mean of the two
+//           sides: B_ij = A sum_l c_ijl kappa_l with c = 1/10 (i = j = l),
+//           1/30 (two equal), 1/60 (all distinct), the exact cubic integral.
 // Cells of one colour share no vertex, so one thread per cell adds its 4x4
 // blocks straight into the CSR values without atomics; colours run in a fixed
 // order, so every sum is formed in the same order on every run.  An interface
@@ -40,6 +48,7 @@ struct AsmArgs {
     const double* invT2_region;
     const double* invT2_cell;  // nullable, 1 per cell (overrides invT2_region)
     const double* kappa_pair;
+    int32_t kappa_cr;      // 1: Crouzeix-Raviart kappa (linear on each side of a facet)
     double *M, *K, *T, *R, *Jx, *Jy, *Jz, *w, *vw;
     int* status;
 };
@@ -54,6 +63,15 @@ __device__ __forceinline__ int32_t find_pos(const int32_t* __restrict__ row_ptr,
         if (v < c) lo = mid + 1; else hi = mid;
     }
     return -1;  // unreachable for a consistent graph
+}
+
+// CR dof of face k of cell c: the region pair's permeability when the cell
+// across the face lies in another region, else 0 (boundary faces too).
+__device__ __forceinline__ double cr_face_kappa(const AsmArgs& a, int32_t c, int k) {
+    const int32_t n = a.nbr[(int64_t)c * 4 + k];
+    if (n < 0) return 0.0;
+    const int rc = a.region[c], rn = a.region[n];
+    return (rc == rn) ? 0.0 : a.kappa_pair[rc * a.n_regions + rn];
 }
 
 __global__ void k_assemble_colour(AsmArgs a) {
@@ -176,6 +194,28 @@ __global__ void k_assemble_colour(AsmArgs a) {
         const double cz = e1[0] * e2[1] - e1[1] * e2[0];
         const double area = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
         const double b = kap * area / 12.0;
+        // Crouzeix-Raviart kappa: the mean of both sides' vertex values on the facet
+        double kv[3] = {0.0, 0.0, 0.0};
+        if (a.kappa_cr) {
+            double kt[4], kn[4], st = 0.0, sn = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                kt[k] = cr_face_kappa(a, t, k);
+                kn[k] = cr_face_kappa(a, nb, k);
+                st += kt[k];
+                sn += kn[k];
+            }
+            const int4 qn = reinterpret_cast<const int4*>(a.tets)[nb];
+            const int32_t vn[4] = {qn.x, qn.y, qn.z, qn.w};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double kb = 0.0;
+#pragma unroll
+                for (int l = 0; l < 4; ++l)
+                    if (vn[l] == v[fv[k]]) kb = sn - 3.0 * kn[l];
+                kv[k] = 0.5 * ((st - 3.0 * kt[fv[k]]) + kb);
+            }
+        }
         int32_t df[3], dg[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -186,7 +226,15 @@ __global__ void k_assemble_colour(AsmArgs a) {
         for (int r = 0; r < 3; ++r)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const double bb = (r == c) ? 2.0 * b : b;
+                double bb = (r == c) ? 2.0 * b : b;
+                if (a.kappa_cr) {
+                    bb = 0.0;
+#pragma unroll
+                    for (int l = 0; l < 3; ++l) {
+                        const int ndist = (r == c) ? ((l == r) ? 1 : 2) : ((l == r || l == c) ? 2 : 3);
+                        bb += area * (ndist == 1 ? 1.0 / 10.0 : (ndist == 2 ? 1.0 / 30.0 : 1.0 / 60.0)) * kv[l];
+                    }
+                }
                 const int32_t p0 = find_pos(a.row_ptr, a.col, df[r], df[c]);
                 const int32_t p1 = find_pos(a.row_ptr, a.col, dg[r], dg[c]);
                 const int32_t p2 = find_pos(a.row_ptr, a.col, df[r], dg[c]);
@@ -286,6 +334,7 @@ void assemble_all(bt_ctx* ctx) {
     a.invT2_region = cf.invT2_region;
     a.invT2_cell = cf.has_cell_T2 ? cf.invT2_cell.p : nullptr;
     a.kappa_pair = cf.kappa_pair;
+    a.kappa_cr = cf.kappa_cr ? 1 : 0;
     a.M = A.M; a.K = A.K; a.T = A.T; a.R = A.R;
     a.Jx = A.Jx; a.Jy = A.Jy; a.Jz = A.Jz;
     a.w = A.w;

@@ -44,6 +44,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <memory>
 
 namespace bt {
 
@@ -66,7 +67,7 @@ struct SolverMixed {
     DevBuf<int32_t> rcomp;
     DevBuf<float2> uh, ul, rh, rl, d0, d1, ri, z, p, q;  // [n][Rp]
     DevBuf<float2> z1, w1, q1;   // [n][Rp]: second buffers of the single-reduction iteration
-    DevBuf<float2> h0, h1, h2;   // per signal [n][Rp/2]: total corrections of the last three steps
+    DevBuf<float2> hc, t1, t2, t3, ex;   // per signal [n][Rp/2]: extrapolated guess (MixArgs)
     DevBuf<float2> partials, fin;   // double-float (hi, lo) sums
     DevBuf<double> sigpart;      // [warps][64][1+kMaxCompartments]
     DevBuf<unsigned> bar;
@@ -119,8 +120,16 @@ struct MixArgs {
     float4* z1;
     float4* w1;
     float4* q1;
-    float2* hist[3];      // per signal: u_{m+1} - u_m of steps m = s-2, s-1, s (rotating by s % 3)
-    int32_t extrap;       // initial guess: 0 u_n, 1 linear, 2 quadratic extrapolation in time
+    // extrapolated initial guess of order extrap (0 u_n, 1 linear ... 4): per signal,
+    // hc = this step's total correction u_{n+1} - u_n (the offset e after phase S),
+    // t1..t3 = backward differences of u at u_n (d_n, d_n - d_{n-1}, ...; own rows
+    // only) and ex = the next step's offset (gathered by phase S)
+    float2* hc;
+    float2* t1;
+    float2* t2;
+    float2* t3;
+    float2* ex;
+    int32_t extrap;
     float2* partials;
     float2* fin;
     double* sigpart;
@@ -226,12 +235,6 @@ __device__ __forceinline__ float2 cdivf(float2 a, float2 b) {
     return make_float2(fmaf(a.x, r, a.y) / d, fmaf(a.y, r, -a.x) / d);
 }
 __device__ __forceinline__ float2 cinvf(float2 b) { return cdivf(make_float2(1.0f, 0.0f), b); }
-// Offset of the extrapolated initial guess from u_n: c1 (u_n - u_{n-1}) + c2 (u_{n-1} - u_{n-2}).
-// The same FP32 expression is used wherever the offset is formed, so the state
-// and the residual see bitwise the same offset.
-__device__ __forceinline__ float2 guess_offset(float2 h1, float2 h2, float c1, float c2) {
-    return make_float2(fmaf(c2, h2.x, c1 * h1.x), fmaf(c2, h2.y, c1 * h1.y));
-}
 __device__ __forceinline__ bool cnonzero(float2 v) {
     return (v.x != 0.0f || v.y != 0.0f) && isfinite(v.x) && isfinite(v.y);
 }
@@ -637,9 +640,9 @@ __device__ __forceinline__ bool inner_single(const MixArgs& a, MixArgs& b, const
                     for (int u = 0; u < W; ++u) {
                         const int c = __shfl_sync(0xffffffffu, my_c, u, LPR);
                         const size_t ni = (size_t)c * Rp4 + c4;
-                        zz[u] = mine ? __ldcg(&Zr[ni]) : f4z;
-                        ww[u] = mine ? __ldcg(&Wr[ni]) : f4z;
-                        qq[u] = mine ? __ldcg(&Qr[ni]) : f4z;
+                        zz[u] = mine ? Zr[ni] : f4z;
+                        ww[u] = mine ? Wr[ni] : f4z;
+                        qq[u] = mine ? Qr[ni] : f4z;
                     }
 #pragma unroll
                     for (int u = 0; u < W; ++u) {
@@ -667,9 +670,9 @@ __device__ __forceinline__ bool inner_single(const MixArgs& a, MixArgs& b, const
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const size_t ni = (size_t)cc[u] * Rp4 + c4;
-                        zz[u] = __ldcg(&Zr[ni]);
-                        ww[u] = __ldcg(&Wr[ni]);
-                        qq[u] = __ldcg(&Qr[ni]);
+                        zz[u] = Zr[ni];
+                        ww[u] = Wr[ni];
+                        qq[u] = Qr[ni];
                     }
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
@@ -680,7 +683,7 @@ __device__ __forceinline__ bool inner_single(const MixArgs& a, MixArgs& b, const
             }
             if (mine) {
                 const size_t vi = (size_t)row * Rp4 + c4;
-                const float4 zo = __ldcg(&Zr[vi]), wo = __ldcg(&Wr[vi]), qo = __ldcg(&Qr[vi]);
+                const float4 zo = Zr[vi], wo = Wr[vi], qo = Qr[vi];
                 const float4 po = P[vi], dd = Dv[vi];
                 const float4 dgr = a.dg[row];
                 float4 qn;
@@ -898,19 +901,26 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             }
             a.rh[vi] = make_float2(re.h, im.h);
             a.rl[vi] = make_float2(re.l, im.l);
+            if (a.extrap > 1 && step > 0) {
+                // backward differences at u_n from the last step's correction d = hc:
+                // t3 <- d - t1 - t2, t2 <- d - t1, t1 <- d (own row, own lane)
+                const float2 dl = __ldcg(&a.hc[vi]), o1 = __ldcg(&a.t1[vi]);
+                if (a.extrap > 2) {
+                    const float2 o2 = __ldcg(&a.t2[vi]);
+                    if (a.extrap > 3) a.t3[vi] = make_float2(dl.x - o1.x - o2.x, dl.y - o1.y - o2.y);
+                    a.t2[vi] = make_float2(dl.x - o1.x, dl.y - o1.y);
+                }
+                a.t1[vi] = dl;
+            }
         }
         // ---- phase S, pass 2 (same rows, same threads: no barrier): start from the
         //      extrapolated guess u_n + e, r -= A e in double-float; the FP32 inner solve
         //      starts from Re(r) (slot 0) and Im(r) (slot 1).  u itself is not written
-        //      here (other threads may still gather u_n in pass 1): e is kept in the
-        //      history slot of this step and added to u by the first phase U.
-        const float c1 = (a.extrap == 0 || step == 0) ? 0.f : ((a.extrap == 1 || step == 1) ? 1.f : 2.f);
-        const float c2 = (a.extrap == 2 && step >= 2) ? -1.f : 0.f;
-        // the history is written inside this kernel: read it coherently (L2), never
-        // through the read-only path
-        const float2* H1 = a.hist[(step + 2) % 3];
-        const float2* H2 = a.hist[(step + 1) % 3];
-        float2* const Hc = a.hist[step % 3];
+        //      here (other threads may still gather u_n in pass 1): e is kept in hc
+        //      and added to u by the first phase U.  e was formed by the last phase U
+        //      of the previous step (ex); it is written inside this kernel, so it is
+        //      read coherently (L2), never through the read-only path.
+        const bool guess = a.extrap > 0 && step > 0;   // uniform over the grid
         KF red[2][kNV];
 #pragma unroll
         for (int j = 0; j < 2; ++j)
@@ -924,12 +934,12 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
 #pragma unroll
             for (int c = 0; c < 2; ++c) ar[c] = jx[c] = jy[c] = jz[c] = DF{0.0f, 0.0f};
             float2 ev = make_float2(0.f, 0.f);
-            if (c1 != 0.0f) {   // uniform over the grid
+            if (guess) {
                 const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
                 for (int e = e0; e < e1; e += 4) {   // four gathers in flight, predicated tail
                     int cc[4];
                     float4 hi[4], lo[4];
-                    float2 h1[4], h2[4];
+                    float2 h1[4];
                     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
@@ -939,14 +949,10 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                         lo[u] = ok ? a.mL[e + u] : z4;
                     }
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const size_t ni = (size_t)cc[u] * Rp4 + c4;
-                        h1[u] = __ldcg(&H1[ni]);
-                        h2[u] = __ldcg(&H2[ni]);
-                    }
+                    for (int u = 0; u < 4; ++u) h1[u] = __ldcg(&a.ex[(size_t)cc[u] * Rp4 + c4]);
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
-                        const float2 en = guess_offset(h1[u], h2[u], c1, c2);
+                        const float2 en = h1[u];
                         const float ec[2] = {en.x, en.y};
 #pragma unroll
                         for (int c = 0; c < 2; ++c) {
@@ -957,7 +963,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                         }
                     }
                 }
-                ev = guess_offset(__ldcg(&H1[vi]), __ldcg(&H2[vi]), c1, c2);
+                ev = __ldcg(&a.ex[vi]);
             }
             DF jg[2];
 #pragma unroll
@@ -973,7 +979,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
             const float2 uhr = a.uh[vi];
             a.rh[vi] = make_float2(re.h, im.h);
             a.rl[vi] = make_float2(re.l, im.l);
-            Hc[vi] = ev;
+            a.hc[vi] = ev;
             const float4 dgr = a.dg[row];
             const float wr = (float)a.w[row] * a.inv_k;
             const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
@@ -1301,9 +1307,9 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 const DF adi = df_add(df_norm(ar[1]), df_scale(jg[0], cn[0]));
                 const DF nr = df_add(DF{rh.x, rl.x}, df_neg(adr));
                 const DF ni = df_add(DF{rh.y, rl.y}, df_neg(adi));
-                // the history slot holds this step's total correction; in the first sweep
-                // it is the guess offset e, which enters u here
-                const float2 hc = Hc[vi];
+                // hc holds this step's total correction; in the first sweep it is the
+                // guess offset e, which enters u here
+                const float2 hc = a.hc[vi];
                 const float2 eo = (sweep == 0) ? hc : make_float2(0.f, 0.f);
                 const DF u_re = df_add(df_add(DF{uh.x, ul.x}, DF{eo.x, 0.0f}), DF{dco[0], 0.0f});
                 const DF u_im = df_add(df_add(DF{uh.y, ul.y}, DF{eo.y, 0.0f}), DF{dco[1], 0.0f});
@@ -1311,7 +1317,31 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 a.rl[vi] = make_float2(nr.l, ni.l);
                 a.uh[vi] = make_float2(u_re.h, u_im.h);
                 a.ul[vi] = make_float2(u_re.l, u_im.l);
-                Hc[vi] = make_float2(hc.x + dco[0], hc.y + dco[1]);
+                const float2 dlt = make_float2(hc.x + dco[0], hc.y + dco[1]);
+                a.hc[vi] = dlt;
+                if (a.extrap > 0) {
+                    // the next step's offset: Newton backward extrapolation of order hp,
+                    // e = hp d - (hp-1) t1 - (hp-2) t2 - (hp-3) t3 with d = u_{n+1} - u_n and
+                    // t1..t3 the differences at u_n (x0 = 3u_{n+1} - 3u_n + u_{n-1} for hp = 2)
+                    const int hp = min(step + 1, a.extrap);
+                    float2 E = make_float2((float)hp * dlt.x, (float)hp * dlt.y);
+                    if (hp >= 2) {
+                        const float2 o1 = __ldcg(&a.t1[vi]);
+                        E.x = fmaf(-(float)(hp - 1), o1.x, E.x);
+                        E.y = fmaf(-(float)(hp - 1), o1.y, E.y);
+                    }
+                    if (hp >= 3) {
+                        const float2 o2 = __ldcg(&a.t2[vi]);
+                        E.x = fmaf(-(float)(hp - 2), o2.x, E.x);
+                        E.y = fmaf(-(float)(hp - 2), o2.y, E.y);
+                    }
+                    if (hp >= 4) {
+                        const float2 o3 = __ldcg(&a.t3[vi]);
+                        E.x -= o3.x;
+                        E.y -= o3.y;
+                    }
+                    a.ex[vi] = E;
+                }
                 const float2 dinv = cinvf(make_float2(dgr.x, cn[0] * (gx[0] * dgr.y + gy[0] * dgr.z + gz[0] * dgr.w)));
                 const float2 z0 = make_float2(dinv.x * nr.h, dinv.y * nr.h);
                 const float2 z1 = make_float2(dinv.x * ni.h, dinv.y * ni.h);
@@ -1599,8 +1629,8 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     for (auto* v : {&W.d0, &W.d1, &W.ri, &W.z, &W.p, &W.q}) v->alloc(nv);        // per slot
     if (single)
         for (auto* v : {&W.z1, &W.w1, &W.q1}) v->alloc(nv);                     // second buffers of z, w~, q~
-    for (auto* v : {&W.uh, &W.ul, &W.rh, &W.rl, &W.h0, &W.h1, &W.h2}) v->alloc(nv / 2);   // per signal
-    for (auto* v : {&W.h0, &W.h1, &W.h2}) v->zero(s);
+    for (auto* v : {&W.uh, &W.ul, &W.rh, &W.rl, &W.hc, &W.t1, &W.t2, &W.t3, &W.ex}) v->alloc(nv / 2);   // per signal
+    for (auto* v : {&W.hc, &W.t1, &W.t2, &W.t3, &W.ex}) v->zero(s);
     W.sig.alloc((size_t)Rp * (1 + kMaxCompartments));
     W.bar.alloc(6);   // [0], [1]: barrier / last-block arrival and release; [2..3]: 64-bit arrival counter;
                       // [4]: never written (stalled_wait)
@@ -1653,9 +1683,11 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     a.z1 = single ? reinterpret_cast<float4*>(W.z1.p) : nullptr;
     a.w1 = single ? reinterpret_cast<float4*>(W.w1.p) : nullptr;
     a.q1 = single ? reinterpret_cast<float4*>(W.q1.p) : nullptr;
-    a.hist[0] = W.h0.p;
-    a.hist[1] = W.h1.p;
-    a.hist[2] = W.h2.p;
+    a.hc = W.hc.p;
+    a.t1 = W.t1.p;
+    a.t2 = W.t2.p;
+    a.t3 = W.t3.p;
+    a.ex = W.ex.p;
     a.extrap = ctx->opt_mixed_extrapolate;
     a.partials = W.partials;
     a.fin = W.fin;
@@ -1695,7 +1727,7 @@ static MixArgs prepare_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int nb
     a.diag = W.diag;
     {
         const void* need_ptrs[] = {a.row_ptr, a.col, a.mA, a.mL, a.mS, a.dg, a.w, a.rcomp, a.uh, a.ul, a.rh, a.rl,
-                                   a.dv[0], a.dv[1], a.ri, a.z, a.p, a.q, a.hist[0], a.hist[1], a.hist[2], a.partials, a.fin, a.sigpart, a.bar,
+                                   a.dv[0], a.dv[1], a.ri, a.z, a.p, a.q, a.hc, a.t1, a.t2, a.t3, a.ex, a.partials, a.fin, a.sigpart, a.bar,
                                    a.status, a.fnew, a.fold, a.qv, a.gv, a.seqv, a.iters, a.sweeps, a.sig, a.diag};
         for (const void* ptr : need_ptrs)
             BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "mixed stepper: a device buffer is not allocated");
@@ -1743,6 +1775,27 @@ struct MixExtra {
     const double* fold = nullptr;
 };
 
+// Apply the adjoint's launch options to prepared arguments (and the initial state).
+static void apply_extra(bt_ctx* ctx, SolverMixed& W, MixArgs& a, const MixExtra* ex) {
+    cudaStream_t s = ctx->stream;
+    const size_t vsz = (size_t)ctx->mesh.n_dofs * (a.Rp / 2);
+    if (ex->zero_init) {
+        W.uh.zero(s);
+        W.ul.zero(s);
+    } else if (ex->init_h) {
+        BT_CUDA(cudaMemcpyAsync(W.uh.p, ex->init_h, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+        BT_CUDA(cudaMemcpyAsync(W.ul.p, ex->init_l, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+    }
+    a.save_h = ex->save_h;
+    a.save_l = ex->save_l;
+    a.save_every = std::max(1, ex->save_every);
+    a.rhs_w = ex->rhs_w;
+    if (ex->fnew) {
+        a.fnew = ex->fnew;
+        a.fold = ex->fold;
+    }
+}
+
 static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_sm_blocks, int blocked, int n_steps,
                           double rtol, int maxit, const double* d_u0, const MixExtra* ex = nullptr) {
     cudaStream_t s = ctx->stream;
@@ -1755,24 +1808,7 @@ static float launch_batch(bt_ctx* ctx, SolverMixed& W, int R, int lpr, int per_s
     const int per_sm = std::max(1, std::min(occ, per_sm_blocks));
     const int nb = std::max(1, std::min(per_sm * ctx->num_sms, blocks_needed(ctx, R, lpr)));
     MixArgs a = prepare_batch(ctx, W, R, lpr, nb, blocked, n_steps, rtol, maxit, d_u0, single);
-    if (ex) {
-        const size_t vsz = (size_t)ctx->mesh.n_dofs * (a.Rp / 2);
-        if (ex->zero_init) {
-            W.uh.zero(s);
-            W.ul.zero(s);
-        } else if (ex->init_h) {
-            BT_CUDA(cudaMemcpyAsync(W.uh.p, ex->init_h, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
-            BT_CUDA(cudaMemcpyAsync(W.ul.p, ex->init_l, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
-        }
-        a.save_h = ex->save_h;
-        a.save_l = ex->save_l;
-        a.save_every = std::max(1, ex->save_every);
-        a.rhs_w = ex->rhs_w;
-        if (ex->fnew) {
-            a.fnew = ex->fnew;
-            a.fold = ex->fold;
-        }
-    }
+    if (ex) apply_extra(ctx, W, a, ex);
     void* args[] = {&a};
     BT_CUDA(cudaEventRecord(ctx->ev1, s));
     BT_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(nb), dim3(kThreadsB), args, 0, s));
@@ -2015,11 +2051,13 @@ static std::vector<int> split_blocks(bt_ctx* const* ctxs, int nm, const std::vec
 
 // One launch of the multi-mesh kernel; returns its device time (ms).
 static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R, int lpr, int n_steps_cap,
-                          double rtol, int maxit, const std::vector<const double*>& d_u0) {
+                          double rtol, int maxit, const std::vector<const double*>& d_u0,
+                          const std::vector<MixExtra>* ex = nullptr) {
     bt_ctx* c0 = ctxs[0];
     cudaStream_t s = c0->stream;
     bool extras = false;
-    for (int m = 0; m < nm; ++m) extras = extras || ctxs[m]->per.on;
+    for (int m = 0; m < nm; ++m)
+        extras = extras || ctxs[m]->per.on || (ex && ((*ex)[m].rhs_w || (*ex)[m].save_h));
     const bool single = !extras && c0->opt_mixed_inner == 1;
     KFnMulti fn = kernel_multi_for(lpr, extras, single);
     int occ = 0;
@@ -2035,6 +2073,7 @@ static float launch_multi(bt_ctx* const* ctxs, int nm, const std::vector<int>& R
         SolverMixed& W = *ctxs[m]->smx;
         const int steps = std::min(n_steps_cap, ctxs[m]->sched.n_steps);
         args[m] = prepare_batch(ctxs[m], W, R[m], lpr, nb[m], 0, steps, rtol, maxit, d_u0[m], single);
+        if (ex) apply_extra(ctxs[m], W, args[m], &(*ex)[m]);
         first[m + 1] = first[m] + nb[m];
     }
     SolverMixed& W0 = *c0->smx;
@@ -2415,22 +2454,33 @@ __global__ void k_adjb_reduce(int64_t n_items, int NS, const int32_t* __restrict
 
 }  // namespace
 
-void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
-                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
-                   bt_stats* st) {
+// One mesh's part of the batched adjoint: its adjoint schedule, cell gradients,
+// interface-facet -> region-pair map, and the per-batch checkpoint, segment,
+// backward-state and accumulator buffers.
+struct AdjMesh {
+    bt_ctx* ctx = nullptr;
+    SolverMixed* W = nullptr;
+    const double* d_u0 = nullptr;
+    int NS = 0, R = 0, Rp = 0, ns = 0;
+    size_t vsz = 0;
+    DevBuf<double> afn, afo, accD, accT, accK, red;
+    DevBuf<float4> cgeo;
+    DevBuf<int32_t> pair;
+    DevBuf<float2> ckh, ckl, sgh, sgl, bkh, bkl, lch, lcl;
+};
+
+static void adj_mesh_setup(AdjMesh& A, bt_ctx* ctx) {
     Mesh& m = ctx->mesh;
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
     BT_REQUIRE(!ctx->coeffs.has_cell_D && !ctx->coeffs.has_cell_T2, BT_ERR_STATE,
-               "bt_adjoint_batch: gradients are defined for per-region coefficients (clear per-cell D / T2)");
-    BT_REQUIRE(!ctx->per.on, BT_ERR_STATE, "bt_adjoint_batch: not defined with pseudo-periodic boundaries");
-    const double* d_u0 = nullptr;
-    SolverMixed& W = pack_mixed(ctx, nullptr, &d_u0);
+               "batched adjoint: gradients are defined for per-region coefficients (clear per-cell D / T2)");
+    BT_REQUIRE(!ctx->per.on, BT_ERR_STATE, "batched adjoint: not defined with pseudo-periodic boundaries");
+    BT_REQUIRE(!ctx->coeffs.kappa_cr, BT_ERR_STATE,
+               "batched adjoint: gradients are defined for one permeability per facet (not the Crouzeix-Raviart mode)");
+    A.ctx = ctx;
+    A.W = &pack_mixed(ctx, nullptr, &A.d_u0);
     const int N = S.n_steps, nr = m.n_regions;
-    const double th = S.theta;
-    if (stride <= 0) stride = (int)std::ceil(std::sqrt((double)N));
-    stride = std::max(1, std::min(stride, N));
-    const int nck = (N + stride - 1) / stride;
     // adjoint schedule: backward step j builds lambda_{N-j} with f_new[N-1-j] and f_old[N-j]
     std::vector<double> afn((size_t)S.n_seq * N), afo((size_t)S.n_seq * N, 0.0);
     for (int r = 0; r < S.n_seq; ++r)
@@ -2438,12 +2488,10 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
             afn[(size_t)r * N + j] = S.f_new[(size_t)r * N + N - 1 - j];
             if (j >= 1) afo[(size_t)r * N + j] = S.f_old[(size_t)r * N + N - j];
         }
-    DevBuf<double> d_afn, d_afo, accD, accT, accK, red;
-    DevBuf<float4> cgeo;
-    d_afn.upload(afn.data(), afn.size(), s);
-    d_afo.upload(afo.data(), afo.size(), s);
-    cgeo.alloc((size_t)m.n_t * 3);
-    k_cell_grad<<<(unsigned)((m.n_t + 127) / 128), 128, 0, s>>>(m.n_t, m.xyz, m.tets, cgeo);
+    A.afn.upload(afn.data(), afn.size(), s);
+    A.afo.upload(afo.data(), afo.size(), s);
+    A.cgeo.alloc((size_t)m.n_t * 3);
+    k_cell_grad<<<(unsigned)((m.n_t + 127) / 128), 128, 0, s>>>(m.n_t, m.xyz, m.tets, A.cgeo);
     BT_CUDA(cudaGetLastError());
     // interface facet -> region pair (r1 <= r2) index r1 * nr + r2
     std::vector<int32_t> hreg(m.n_t), hpair(std::max<int64_t>(1, m.n_iface), 0);
@@ -2459,129 +2507,223 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
             hpair[i] = std::min(hreg[t], hreg[nb]) * nr + std::max(hreg[t], hreg[nb]);
         }
     }
-    DevBuf<int32_t> pair;
-    pair.upload(hpair.data(), hpair.size(), s);
+    A.pair.upload(hpair.data(), hpair.size(), s);
+}
+
+// Buffers of one batch of NS signals padded to Rp slots, and checkpoint 0 (u0 = 1).
+static void adj_batch_alloc(AdjMesh& A, int NS, int Rp, int nck, int stride) {
+    Mesh& m = A.ctx->mesh;
+    cudaStream_t s = A.ctx->stream;
+    SolverMixed& W = *A.W;
+    A.NS = NS;
+    A.R = 2 * NS;
+    A.Rp = Rp;
+    A.ns = Rp / 2;
+    A.vsz = (size_t)m.n_dofs * A.ns;
+    const size_t vsz = A.vsz;
+    A.ckh.alloc((nck + 1) * vsz); A.ckl.alloc((nck + 1) * vsz);
+    A.sgh.alloc((stride + 1) * vsz); A.sgl.alloc((stride + 1) * vsz);
+    A.bkh.alloc(stride * vsz); A.bkl.alloc(stride * vsz);
+    A.lch.alloc(vsz); A.lcl.alloc(vsz);
+    A.accD.alloc((size_t)m.n_t * NS); A.accD.zero(s);
+    A.accT.alloc((size_t)m.n_t * NS); A.accT.zero(s);
+    A.accK.alloc((size_t)std::max<int64_t>(1, m.n_iface) * NS); A.accK.zero(s);
+    k_rows_mixed<<<(unsigned)((m.n_dofs + 255) / 256), 256, 0, s>>>(m.n_dofs, Rp, A.R, m.diag_pos, W.mA, A.ctx->mat.w,
+                                                                    m.dof_comp, m.dof_vertex, nullptr, W.dg, W.w,
+                                                                    W.rcomp, A.ckh.p, A.ckl.p);
+    BT_CUDA(cudaGetLastError());
+}
+
+// Contractions of backward step n of one mesh (states u_n, u_{n+1} of the segment
+// starting at a0, lambda_{n+1}).
+static void adj_contract(AdjMesh& A, int n, int a0, int e0, double theta) {
+    Mesh& m = A.ctx->mesh;
+    cudaStream_t s = A.ctx->stream;
+    const size_t vsz = A.vsz;
+    const float2* Lh = (n + 1 == e0) ? A.lch.p : A.bkh.p + (size_t)(e0 - 2 - n) * vsz;
+    const float2* Ll = (n + 1 == e0) ? A.lcl.p : A.bkl.p + (size_t)(e0 - 2 - n) * vsz;
+    const size_t o0 = (size_t)(n - a0) * vsz, o1 = o0 + vsz;
+    const unsigned cb = (unsigned)((m.n_t * A.NS + 255) / 256), fb = (unsigned)((m.n_iface * A.NS + 255) / 256);
+    k_adjb_cells<<<cb, 256, 0, s>>>(m.n_t, A.NS, A.ns, A.cgeo, m.tets, m.comp, m.dof_of, m.n_comp, Lh, Ll,
+                                    A.sgh.p + o0, A.sgl.p + o0, A.sgh.p + o1, A.sgl.p + o1, theta, A.accD, A.accT);
+    if (m.n_iface > 0)
+        k_adjb_facets<<<fb, 256, 0, s>>>(m.n_iface, A.NS, A.ns, m.iface_cell, m.iface_face, m.xyz, m.tets, m.nbr,
+                                         m.comp, m.dof_of, m.n_comp, Lh, Ll, A.sgh.p + o0, A.sgl.p + o0,
+                                         A.sgh.p + o1, A.sgl.p + o1, theta, A.accK);
+    BT_CUDA(cudaGetLastError());
+}
+
+// Per-signal sums over regions and region pairs (fixed order) into the outputs of
+// signals [b0, b0 + NS) of this mesh.
+static void adj_finish(AdjMesh& A, int b0, double* dD, double* dinvT2, double* dkappa) {
+    Mesh& m = A.ctx->mesh;
+    cudaStream_t s = A.ctx->stream;
+    const int NS = A.NS, nr = m.n_regions;
+    A.red.alloc((size_t)NS * (2 * nr + nr * nr));
+    k_adjb_reduce<<<dim3(NS, nr), 256, 0, s>>>(m.n_t, NS, m.region, nr, A.accD, A.red.p);
+    k_adjb_reduce<<<dim3(NS, nr), 256, 0, s>>>(m.n_t, NS, m.region, nr, A.accT, A.red.p + (size_t)NS * nr);
+    if (m.n_iface > 0)
+        k_adjb_reduce<<<dim3(NS, nr * nr), 256, 0, s>>>(m.n_iface, NS, A.pair, nr * nr, A.accK,
+                                                       A.red.p + (size_t)2 * NS * nr);
+    BT_CUDA(cudaGetLastError());
+    std::vector<double> hr((size_t)NS * (2 * nr + nr * nr), 0.0);
+    A.red.download(hr.data(), (size_t)NS * (2 * nr + (m.n_iface > 0 ? nr * nr : 0)), s);
+    BT_CUDA(cudaStreamSynchronize(s));
+    for (int sg = 0; sg < NS; ++sg) {
+        const size_t o = (size_t)(b0 + sg);
+        for (int r = 0; r < nr; ++r) {
+            if (dD) dD[o * nr + r] = hr[(size_t)sg * nr + r];
+            if (dinvT2) dinvT2[o * nr + r] = hr[(size_t)NS * nr + (size_t)sg * nr + r];
+        }
+        if (dkappa)
+            for (int r1 = 0; r1 < nr; ++r1)
+                for (int r2 = 0; r2 < nr; ++r2) {
+                    const int a = std::min(r1, r2), b = std::max(r1, r2);
+                    dkappa[o * nr * nr + (size_t)r1 * nr + r2] =
+                        (a == b) ? 0.0 : hr[(size_t)2 * NS * nr + (size_t)sg * nr * nr + (size_t)a * nr + b];
+                }
+    }
+}
+
+// The adjoint pipeline of a group of meshes (one batch each) whose launches are
+// shared: launch(n_steps, ex) runs one launch of every mesh in the group with the
+// per-mesh extras ex[g] and returns its device time.  All meshes have N steps.
+template <typename Launch>
+static void adj_pipeline(std::vector<AdjMesh*>& G, int N, int stride, double theta, Launch&& launch,
+                         const std::vector<int>& b0, const std::vector<double*>& sig, float& ms,
+                         int64_t& launches) {
+    const int ng = (int)G.size();
+    const int nck = (N + stride - 1) / stride;
+    std::vector<MixExtra> ex(ng);
+    {   // forward: u_{j stride} into checkpoint j, and the signals
+        for (int g = 0; g < ng; ++g) {
+            ex[g] = MixExtra();
+            ex[g].save_h = G[g]->ckh.p + G[g]->vsz;
+            ex[g].save_l = G[g]->ckl.p + G[g]->vsz;
+            ex[g].save_every = stride;
+        }
+        ms += launch(N, ex);
+        ++launches;
+        for (int g = 0; g < ng; ++g)
+            collect_batch(G[g]->ctx, *G[g]->W, b0[g], G[g]->NS, false, sig[g] + b0[g], nullptr, nullptr);
+    }
+    {   // lambda_N = A_{N-1}^{-1} w from the zero state
+        for (int g = 0; g < ng; ++g) {
+            ex[g] = MixExtra();
+            ex[g].zero_init = true;
+            ex[g].rhs_w = 1;
+            ex[g].fnew = G[g]->afn.p;
+            ex[g].fold = G[g]->afo.p;
+        }
+        ms += launch(1, ex);
+        ++launches;
+        for (int g = 0; g < ng; ++g) {
+            AdjMesh& A = *G[g];
+            cudaStream_t s = A.ctx->stream;
+            BT_CUDA(cudaMemcpyAsync(A.lch.p, A.W->uh.p, A.vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+            BT_CUDA(cudaMemcpyAsync(A.lcl.p, A.W->ul.p, A.vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    for (int sgm = nck - 1; sgm >= 0; --sgm) {
+        const int a0 = sgm * stride, e0 = std::min(a0 + stride, N), len = e0 - a0;
+        for (int g = 0; g < ng; ++g) {   // u_{a0..e0}: seg[k] = u_{a0+k}
+            AdjMesh& A = *G[g];
+            cudaStream_t s = A.ctx->stream;
+            BT_CUDA(cudaMemcpyAsync(A.sgh.p, A.ckh.p + (size_t)sgm * A.vsz, A.vsz * sizeof(float2),
+                                    cudaMemcpyDeviceToDevice, s));
+            BT_CUDA(cudaMemcpyAsync(A.sgl.p, A.ckl.p + (size_t)sgm * A.vsz, A.vsz * sizeof(float2),
+                                    cudaMemcpyDeviceToDevice, s));
+            ex[g] = MixExtra();
+            ex[g].init_h = A.sgh.p;
+            ex[g].init_l = A.sgl.p;
+            ex[g].save_h = A.sgh.p + A.vsz;
+            ex[g].save_l = A.sgl.p + A.vsz;
+            ex[g].fnew = A.W->fnew.p + a0;
+            ex[g].fold = A.W->fold.p + a0;
+        }
+        ms += launch(len, ex);
+        ++launches;
+        // lambda_{e0-1} ... lambda_{a0} (lambda_0 is not needed): bk[k] = lambda_{e0-1-k}
+        const int nb_steps = (a0 == 0) ? len - 1 : len;
+        if (nb_steps > 0) {
+            for (int g = 0; g < ng; ++g) {
+                AdjMesh& A = *G[g];
+                ex[g] = MixExtra();
+                ex[g].init_h = A.lch.p;
+                ex[g].init_l = A.lcl.p;
+                ex[g].save_h = A.bkh.p;
+                ex[g].save_l = A.bkl.p;
+                ex[g].fnew = A.afn.p + (N - e0 + 1);
+                ex[g].fold = A.afo.p + (N - e0 + 1);
+            }
+            ms += launch(nb_steps, ex);
+            ++launches;
+        }
+        for (int g = 0; g < ng; ++g) {
+            AdjMesh& A = *G[g];
+            for (int n = e0 - 1; n >= a0; --n) {
+                adj_contract(A, n, a0, e0, theta);
+                launches += 1 + (A.ctx->mesh.n_iface > 0);
+            }
+            if (a0 > 0) {   // lambda_{a0} starts the previous segment
+                cudaStream_t s = A.ctx->stream;
+                BT_CUDA(cudaMemcpyAsync(A.lch.p, A.bkh.p + (size_t)(len - 1) * A.vsz, A.vsz * sizeof(float2),
+                                        cudaMemcpyDeviceToDevice, s));
+                BT_CUDA(cudaMemcpyAsync(A.lcl.p, A.bkl.p + (size_t)(len - 1) * A.vsz, A.vsz * sizeof(float2),
+                                        cudaMemcpyDeviceToDevice, s));
+            }
+        }
+    }
+}
+
+static int adj_stride(int N, int stride) {
+    if (stride <= 0) stride = (int)std::ceil(std::sqrt((double)N));
+    return std::max(1, std::min(stride, N));
+}
+
+void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
+                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
+                   bt_stats* st) {
+    Schedule& S = ctx->sched;
+    cudaStream_t s = ctx->stream;
+    AdjMesh A;
+    adj_mesh_setup(A, ctx);
+    SolverMixed& W = *A.W;
+    const int N = S.n_steps;
+    stride = adj_stride(N, stride);
+    const int nck = (N + stride - 1) / stride;
     reset_stats(st, N, rtol);
     ctx->last_iters.assign((size_t)nsig * N, 0);   // collect_batch records the forward sweep's counts
     W.saved.clear();
     W.saved_nsig = 0;
     float ms = 0.0f;
     int64_t launches = 1;
+    // signals per set of launches: at most 256, and few enough that the checkpoint,
+    // segment and backward states (a double-float complex value per dof each) and
+    // the accumulators of a batch take at most a quarter of the free device memory
+    // (the RHS padding can double the states)
+    int cap = kMaxRhs / 2;
+    {
+        size_t free_b = 0, total_b = 0;
+        BT_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const Mesh& m = ctx->mesh;
+        const double per_sig = (double)((nck + 1) + (stride + 1) + stride + 1) * 16.0 * (double)m.n_dofs +
+                               8.0 * (2.0 * (double)m.n_t + (double)std::max<int64_t>(1, m.n_iface));
+        cap = (int)std::max(1.0, std::min((double)cap, 0.25 * (double)free_b / per_sig));
+    }
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
-    for (int32_t b0 = 0; b0 < nsig; b0 += kMaxRhs / 2) {
-        const int NS = std::min<int32_t>(kMaxRhs / 2, nsig - b0);
+    for (int32_t b0 = 0; b0 < nsig; b0 += cap) {
+        const int NS = std::min<int32_t>(cap, nsig - b0);
         const int R = 2 * NS;
         upload_rhs(ctx, W, NS, q + b0, gdir + 3 * b0, seq ? seq + b0 : nullptr);
-        const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, d_u0);
-        const int Rp = padded_rhs(R, geo.lpr), ns = Rp / 2;
-        const size_t vsz = (size_t)m.n_dofs * ns;
-        DevBuf<float2> ckh, ckl, sgh, sgl, bkh, bkl, lch, lcl;
-        ckh.alloc((nck + 1) * vsz); ckl.alloc((nck + 1) * vsz);
-        sgh.alloc((stride + 1) * vsz); sgl.alloc((stride + 1) * vsz);
-        bkh.alloc(stride * vsz); bkl.alloc(stride * vsz);
-        lch.alloc(vsz); lcl.alloc(vsz);
-        accD.alloc((size_t)m.n_t * NS); accD.zero(s);
-        accT.alloc((size_t)m.n_t * NS); accT.zero(s);
-        accK.alloc((size_t)std::max<int64_t>(1, m.n_iface) * NS); accK.zero(s);
-        auto run = [&](int n_steps, const MixExtra& ex) {
-            ms += launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, n_steps, rtol, maxit, d_u0, &ex);
-            ++launches;
+        const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, A.d_u0);
+        adj_batch_alloc(A, NS, padded_rhs(R, geo.lpr), nck, stride);
+        std::vector<AdjMesh*> G{&A};
+        auto launch = [&](int n_steps, const std::vector<MixExtra>& ex) {
+            return launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, n_steps, rtol, maxit, A.d_u0, &ex[0]);
         };
-        // checkpoint 0: the initial state (u0 = 1), in the batch's layout
-        k_rows_mixed<<<(unsigned)((m.n_dofs + 255) / 256), 256, 0, s>>>(m.n_dofs, Rp, R, m.diag_pos, W.mA,
-                                                                        ctx->mat.w, m.dof_comp, m.dof_vertex,
-                                                                        nullptr, W.dg, W.w, W.rcomp, ckh.p, ckl.p);
-        BT_CUDA(cudaGetLastError());
-        {   // forward: u_{j stride} into checkpoint j, and the signals
-            MixExtra ex;
-            ex.save_h = ckh.p + vsz;
-            ex.save_l = ckl.p + vsz;
-            ex.save_every = stride;
-            run(N, ex);
-            collect_batch(ctx, W, b0, NS, false, sig + b0, nullptr, nullptr);
-        }
-        {   // lambda_N = A_{N-1}^{-1} w from the zero state
-            MixExtra ex;
-            ex.zero_init = true;
-            ex.rhs_w = 1;
-            ex.fnew = d_afn.p;
-            ex.fold = d_afo.p;
-            run(1, ex);
-            BT_CUDA(cudaMemcpyAsync(lch.p, W.uh.p, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
-            BT_CUDA(cudaMemcpyAsync(lcl.p, W.ul.p, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
-        }
-        const unsigned cb = (unsigned)((m.n_t * NS + 255) / 256), fb = (unsigned)((m.n_iface * NS + 255) / 256);
-        for (int sgm = nck - 1; sgm >= 0; --sgm) {
-            const int a0 = sgm * stride, e0 = std::min(a0 + stride, N), len = e0 - a0;
-            // u_{a0..e0}: seg[k] = u_{a0+k}
-            BT_CUDA(cudaMemcpyAsync(sgh.p, ckh.p + (size_t)sgm * vsz, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
-            BT_CUDA(cudaMemcpyAsync(sgl.p, ckl.p + (size_t)sgm * vsz, vsz * sizeof(float2), cudaMemcpyDeviceToDevice, s));
-            {
-                MixExtra ex;
-                ex.init_h = sgh.p;
-                ex.init_l = sgl.p;
-                ex.save_h = sgh.p + vsz;
-                ex.save_l = sgl.p + vsz;
-                ex.fnew = W.fnew.p + a0;
-                ex.fold = W.fold.p + a0;
-                run(len, ex);
-            }
-            // lambda_{e0-1} ... lambda_{a0} (lambda_0 is not needed): bk[k] = lambda_{e0-1-k}
-            const int nb_steps = (a0 == 0) ? len - 1 : len;
-            if (nb_steps > 0) {
-                MixExtra ex;
-                ex.init_h = lch.p;
-                ex.init_l = lcl.p;
-                ex.save_h = bkh.p;
-                ex.save_l = bkl.p;
-                ex.fnew = d_afn.p + (N - e0 + 1);
-                ex.fold = d_afo.p + (N - e0 + 1);
-                run(nb_steps, ex);
-            }
-            for (int n = e0 - 1; n >= a0; --n) {
-                const float2* Lh = (n + 1 == e0) ? lch.p : bkh.p + (size_t)(e0 - 2 - n) * vsz;
-                const float2* Ll = (n + 1 == e0) ? lcl.p : bkl.p + (size_t)(e0 - 2 - n) * vsz;
-                const size_t o0 = (size_t)(n - a0) * vsz, o1 = o0 + vsz;
-                k_adjb_cells<<<cb, 256, 0, s>>>(m.n_t, NS, ns, cgeo, m.tets, m.comp, m.dof_of, m.n_comp, Lh, Ll,
-                                                sgh.p + o0, sgl.p + o0, sgh.p + o1, sgl.p + o1, th, accD, accT);
-                if (m.n_iface > 0)
-                    k_adjb_facets<<<fb, 256, 0, s>>>(m.n_iface, NS, ns, m.iface_cell, m.iface_face, m.xyz, m.tets,
-                                                     m.nbr, m.comp, m.dof_of, m.n_comp, Lh, Ll, sgh.p + o0,
-                                                     sgl.p + o0, sgh.p + o1, sgl.p + o1, th, accK);
-                BT_CUDA(cudaGetLastError());
-            }
-            if (a0 > 0) {   // lambda_{a0} starts the previous segment
-                BT_CUDA(cudaMemcpyAsync(lch.p, bkh.p + (size_t)(len - 1) * vsz, vsz * sizeof(float2),
-                                        cudaMemcpyDeviceToDevice, s));
-                BT_CUDA(cudaMemcpyAsync(lcl.p, bkl.p + (size_t)(len - 1) * vsz, vsz * sizeof(float2),
-                                        cudaMemcpyDeviceToDevice, s));
-            }
-        }
-        // per-signal sums over regions and region pairs, in a fixed order
-        red.alloc((size_t)NS * (2 * nr + nr * nr));
-        k_adjb_reduce<<<dim3(NS, nr), 256, 0, s>>>(m.n_t, NS, m.region, nr, accD, red.p);
-        k_adjb_reduce<<<dim3(NS, nr), 256, 0, s>>>(m.n_t, NS, m.region, nr, accT, red.p + (size_t)NS * nr);
-        if (m.n_iface > 0)
-            k_adjb_reduce<<<dim3(NS, nr * nr), 256, 0, s>>>(m.n_iface, NS, pair, nr * nr, accK,
-                                                           red.p + (size_t)2 * NS * nr);
-        BT_CUDA(cudaGetLastError());
-        std::vector<double> hr((size_t)NS * (2 * nr + nr * nr), 0.0);
-        red.download(hr.data(), (size_t)NS * (2 * nr + (m.n_iface > 0 ? nr * nr : 0)), s);
-        BT_CUDA(cudaStreamSynchronize(s));
-        for (int sg = 0; sg < NS; ++sg) {
-            const size_t o = (size_t)(b0 + sg);
-            for (int r = 0; r < nr; ++r) {
-                if (dD) dD[o * nr + r] = hr[(size_t)sg * nr + r];
-                if (dinvT2) dinvT2[o * nr + r] = hr[(size_t)NS * nr + (size_t)sg * nr + r];
-            }
-            if (dkappa)
-                for (int r1 = 0; r1 < nr; ++r1)
-                    for (int r2 = 0; r2 < nr; ++r2) {
-                        const int a = std::min(r1, r2), b = std::max(r1, r2);
-                        dkappa[o * nr * nr + (size_t)r1 * nr + r2] =
-                            (a == b) ? 0.0 : hr[(size_t)2 * NS * nr + (size_t)sg * nr * nr + (size_t)a * nr + b];
-                    }
-        }
+        adj_pipeline(G, N, stride, S.theta, launch, {(int)b0}, {sig}, ms, launches);
+        adj_finish(A, b0, dD, dinvT2, dkappa);
     }
     BT_CUDA(cudaEventRecord(ctx->ev2, s));
     BT_CUDA(cudaEventSynchronize(ctx->ev2));
@@ -2592,6 +2734,139 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
         st->stepper_ms = ms;
         st->kernel_launches = launches;
     }
+}
+
+// The batched adjoint of several meshes in one call.  Meshes whose batch fills
+// the GPU run alone (adjoint_mixed); the others share every launch of the
+// pipeline (forward with checkpoints, the w step, segment recomputes, backward
+// segments), each mesh with its own sub-grid, barriers and reductions, so small
+// meshes do not each pay a whole-GPU launch per phase.
+void adjoint_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q, const double* gdir,
+                         const int32_t* seq, double rtol, int32_t maxit, int32_t stride, double* sig, double* dD,
+                         double* dinvT2, double* dkappa, bt_stats* st) {
+    bt_ctx* c0 = ctxs[0];
+    cudaStream_t s = c0->stream;
+    const int N = c0->sched.n_steps;
+    for (int m = 0; m < nm; ++m)
+        BT_REQUIRE(ctxs[m]->sched.n_steps == N && ctxs[m]->sched.theta == c0->sched.theta, BT_ERR_INVALID,
+                   "bt_adjoint_multi: every mesh needs the same number of time steps and theta");
+    stride = adj_stride(N, stride);
+    const int nck = (N + stride - 1) / stride;
+    // every mesh's work goes on the first context's stream for this call
+    std::vector<cudaStream_t> saved(nm);
+    for (int m = 0; m < nm; ++m) {
+        BT_CUDA(cudaStreamSynchronize(ctxs[m]->stream));
+        saved[m] = ctxs[m]->stream;
+        ctxs[m]->stream = s;
+    }
+    struct Restore {
+        bt_ctx* const* c;
+        std::vector<cudaStream_t>& v;
+        ~Restore() {
+            for (size_t m = 0; m < v.size(); ++m) c[m]->stream = v[m];
+        }
+    } restore{ctxs, saved};
+    std::vector<int64_t> off(nm + 1, 0), offr(nm + 1, 0), offk(nm + 1, 0);
+    for (int m = 0; m < nm; ++m) {
+        const int nr = ctxs[m]->mesh.n_regions;
+        off[m + 1] = off[m] + nsig[m];
+        offr[m + 1] = offr[m] + (int64_t)nsig[m] * nr;
+        offk[m + 1] = offk[m] + (int64_t)nsig[m] * nr * nr;
+    }
+    std::vector<int> small, large;
+    for (int m = 0; m < nm; ++m) {
+        const int64_t units = ctxs[m]->mesh.n_dofs * (int64_t)ceil_pow2(2 * nsig[m]) / 64;
+        (units / kWarpsB >= 2 * ctxs[m]->num_sms ? large : small).push_back(m);
+    }
+    if (small.size() == 1) {
+        large.push_back(small[0]);
+        small.clear();
+    }
+    reset_stats(st, N, rtol);
+    BT_CUDA(cudaEventRecord(c0->ev3, s));
+    for (int m : large) {
+        bt_stats one{};
+        adjoint_mixed(ctxs[m], nsig[m], q + off[m], gdir + 3 * off[m], seq ? seq + off[m] : nullptr, rtol, maxit,
+                      stride, sig + off[m], dD ? dD + offr[m] : nullptr, dinvT2 ? dinvT2 + offr[m] : nullptr,
+                      dkappa ? dkappa + offk[m] : nullptr, &one);
+        add_stats(st, one);
+    }
+    if (!small.empty()) {
+        const int ng = (int)small.size();
+        std::vector<bt_ctx*> cs;
+        std::vector<int> R;
+        std::vector<const double*> u0s(ng, nullptr);
+        std::vector<std::unique_ptr<AdjMesh>> As;
+        for (int m : small) {
+            cs.push_back(ctxs[m]);
+            R.push_back(2 * nsig[m]);
+            As.emplace_back(new AdjMesh());
+            adj_mesh_setup(*As.back(), ctxs[m]);
+            upload_rhs(ctxs[m], *As.back()->W, nsig[m], q + off[m], gdir + 3 * off[m], seq ? seq + off[m] : nullptr);
+            ctxs[m]->last_iters.assign((size_t)nsig[m] * N, 0);
+            As.back()->W->saved.clear();
+            As.back()->W->saved_nsig = 0;
+        }
+        // a lanes-per-row every mesh's batch can use: the choice bt_solve_multi made
+        // for this set of meshes and batch sizes, else the fastest on 3-step runs
+        std::vector<int> cands;
+        for (int c = 1; c <= 32; c <<= 1) {
+            bool ok = true;
+            for (int g = 0; g < ng; ++g) ok = ok && padded_rhs(R[g], c) > 0;
+            if (ok) cands.push_back(c);
+        }
+        if (cs[0]->opt_mixed_lpr > 0) cands = {cs[0]->opt_mixed_lpr};
+        BT_REQUIRE(!cands.empty(), BT_ERR_INVALID, "bt_adjoint_multi: no lanes-per-row fits every mesh's batch");
+        int lpr = cands[0];
+        std::vector<int64_t> key;
+        for (int g = 0; g < ng; ++g) {
+            key.push_back(cs[g]->mesh.n_dofs);
+            key.push_back(R[g]);
+        }
+        SolverMixed& Wc = *cs[0]->smx;
+        auto hit = Wc.tuned_multi.find(key);
+        if (cs[0]->opt_mixed_lpr <= 0 && hit != Wc.tuned_multi.end()) {
+            lpr = hit->second;
+        } else if (cands.size() > 1) {
+            float best = 1e30f;
+            for (int c : cands) {
+                const float t = launch_multi(cs.data(), ng, R, c, 3, rtol, maxit, u0s);
+                if (t < best) {
+                    best = t;
+                    lpr = c;
+                }
+            }
+            Wc.tuned_multi[key] = lpr;
+        }
+        std::vector<AdjMesh*> G;
+        std::vector<int> b0(ng, 0);
+        std::vector<double*> sg(ng);
+        for (int g = 0; g < ng; ++g) {
+            adj_batch_alloc(*As[g], nsig[small[g]], padded_rhs(R[g], lpr), nck, stride);
+            G.push_back(As[g].get());
+            sg[g] = sig + off[small[g]];
+        }
+        float ms = 0.0f;
+        int64_t launches = 0;
+        auto launch = [&](int n_steps, const std::vector<MixExtra>& ex) {
+            return launch_multi(cs.data(), ng, R, lpr, n_steps, rtol, maxit, u0s, &ex);
+        };
+        adj_pipeline(G, N, stride, c0->sched.theta, launch, b0, sg, ms, launches);
+        for (int g = 0; g < ng; ++g) {
+            const int m = small[g];
+            adj_finish(*As[g], 0, dD ? dD + offr[m] : nullptr, dinvT2 ? dinvT2 + offr[m] : nullptr,
+                       dkappa ? dkappa + offk[m] : nullptr);
+        }
+        if (st) {
+            st->stepper_ms += ms;
+            st->kernel_launches += launches;
+        }
+    }
+    BT_CUDA(cudaEventRecord(c0->ev2, s));
+    BT_CUDA(cudaEventSynchronize(c0->ev2));
+    float total = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&total, c0->ev3, c0->ev2));
+    if (st) st->gpu_ms = total;
 }
 
 }  // namespace bt

@@ -131,6 +131,7 @@ struct Coeffs {
     DevBuf<double> D_region, invT2_region, kappa_pair, D_cell, invT2_cell;
     bool has_cell_D = false;
     bool has_cell_T2 = false;
+    bool kappa_cr = false;   // Crouzeix-Raviart (per-facet linear) permeability
     bool set = false;
 };
 
@@ -198,7 +199,7 @@ struct bt_ctx {
     int opt_mixed_max_sweeps = 8;
     double opt_mixed_eps_first = 3e-6;
     double opt_mixed_eps_next = 1e-2;
-    int opt_mixed_extrapolate = 2;
+    int opt_mixed_extrapolate = 4;   // order of the mixed path's extrapolated initial guess (0..4)
     int opt_mixed_blocked = -1;
     int opt_mixed_reduce = -1;
     double opt_mixed_growth2 = 1e8;   // divergence guard of a sweep (squared-norm growth over its minimum)
@@ -237,6 +238,9 @@ void set_periodic(bt_ctx* ctx, const int32_t* dir);
 void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
                    int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
                    bt_stats* st);
+void adjoint_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q, const double* gdir,
+                         const int32_t* seq, double rtol, int32_t maxit, int32_t stride, double* sig, double* dD,
+                         double* dinvT2, double* dkappa, bt_stats* st);
 
 void free_solvers(bt_ctx* ctx);
 double device_sum(const double* d, int64_t n, cudaStream_t s);

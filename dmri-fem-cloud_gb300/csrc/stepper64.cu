@@ -824,6 +824,8 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
                "bt_adjoint: gradients are defined for per-region 1/T2 (clear the per-cell T2)");
     BT_REQUIRE(!ctx->per.on, BT_ERR_STATE,
                "bt_adjoint: not defined with pseudo-periodic boundaries (the mirror term is not transposed)");
+    BT_REQUIRE(!ctx->coeffs.kappa_cr, BT_ERR_STATE,
+               "bt_adjoint: gradients are defined for one permeability per facet (not the Crouzeix-Raviart mode)");
     if (!ctx->s64) ctx->s64 = new Solver64();
     Solver64& W = *ctx->s64;
     prepare_fp64(ctx, W);
@@ -1008,6 +1010,8 @@ void tangent_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
     BT_REQUIRE(!ctx->coeffs.has_cell_D && !ctx->coeffs.has_cell_T2, BT_ERR_STATE,
                "bt_tangent: derivatives are defined for per-region coefficients (clear per-cell D / T2)");
     BT_REQUIRE(!ctx->per.on, BT_ERR_STATE, "bt_tangent: not defined with pseudo-periodic boundaries");
+    BT_REQUIRE(!ctx->coeffs.kappa_cr, BT_ERR_STATE,
+               "bt_tangent: derivatives are defined for one permeability per facet (not the Crouzeix-Raviart mode)");
     const int nr = m.n_regions;
     BT_REQUIRE(kind >= 0 && kind <= 2 && ri >= 0 && ri < nr && (kind != 2 || (rj >= 0 && rj < nr && rj != ri)),
                BT_ERR_INVALID, "bt_tangent: bad parameter");

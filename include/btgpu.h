@@ -125,6 +125,20 @@ int bt_mesh_info(bt_ctx* ctx, bt_mesh_info_t* out);
 int bt_set_coefficients(bt_ctx* ctx, const double* D_region, const double* invT2_region,
                         const double* kappa_pair);
 
+/* How the permeability enters the interface term kappa int_F [u][v] (icondition_wBC,
+ * DmriFemLib.py:47-50): BT_KAPPA_FACET (default) uses the region pair's value,
+ * constant on each interface facet (GCloudDmriSolver.py:204); BT_KAPPA_CR is the
+ * reference's per-interface permeability as a Crouzeix-Raviart function
+ * (MultilayeredDiskVariablePermeability.ipynb:480-502): the CR dof of every
+ * interior facet is kappa_pair of its two regions where they differ, else 0, so
+ * on a facet whose cell has another interface facet (staircase corners) kappa is
+ * linear, not constant; the facet integral is then exact cubic.  Takes effect at
+ * the next bt_assemble; bt_mesh_upload resets it.  The adjoints and bt_tangent
+ * reject the CR mode. */
+#define BT_KAPPA_FACET 0
+#define BT_KAPPA_CR 1
+int bt_set_kappa_mode(bt_ctx* ctx, int32_t mode);
+
 /* Optional anisotropic per-cell D: D_cell[n_cells*6] = (xx, yy, zz, xy, xz, yz)
  * (ImposeDiffusionTensor, DmriFemLib.py:611-616, symmetric part).  NULL
  * clears it (back to D_region). */
@@ -222,12 +236,30 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  * sweep is a forward sweep of the same kernel with the schedule pair
  * f_new[n-1], f_old[n]): signal_out[n_signals], dS_dD[n_signals*n_regions],
  * dS_dinvT2[n_signals*n_regions], dS_dkappa[n_signals*n_regions*n_regions]
- * (signal-major, as bt_adjoint per signal).  u0 = 1.  Up to 128 signals share
- * one set of launches; more are processed in groups.  Any output pointer but
- * signal_out may be NULL. */
+ * (signal-major, as bt_adjoint per signal).  u0 = 1.  Up to 256 signals share
+ * one set of launches -- fewer when their checkpoint, segment and backward
+ * states would take more than a quarter of the free device memory; more are
+ * processed in groups.  Any output pointer but signal_out may be NULL. */
 int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir,
                      const int32_t* sequence, double rtol, int32_t max_iterations, int32_t checkpoint_stride,
                      double* signal_out, double* dS_dD, double* dS_dinvT2, double* dS_dkappa, bt_stats* stats);
+
+/* bt_adjoint_batch for several meshes in one call: mesh m is the mesh,
+ * coefficients, assembly and schedule of contexts[m] (all with the same number
+ * of steps and theta) and gets n_signals[m] (1..256) signals; q, gdir, sequence
+ * and signal_out list the signals mesh by mesh, and the gradients are
+ * concatenated mesh by mesh in bt_adjoint_batch's layout: dS_dD and dS_dinvT2
+ * hold n_signals[m] * n_regions(m) values per mesh, dS_dkappa n_signals[m] *
+ * n_regions(m)^2.  Meshes whose batch fills the GPU run alone; the others share
+ * every launch of the adjoint (forward with checkpoints, the w step, segment
+ * recomputes and backward segments), each with its own sub-grid.  All work runs
+ * on the first context's stream; at most 64 meshes.  The reference has no
+ * adjoint: its gradients would be finite differences of one GCloudDmriSolver.py
+ * job per mesh (GCloudDmriSolver.py:232, DmriFemLib.py:878-915). */
+int bt_adjoint_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_signals, const double* q,
+                     const double* gdir, const int32_t* sequence, double rtol, int32_t max_iterations,
+                     int32_t checkpoint_stride, double* signal_out, double* dS_dD, double* dS_dinvT2,
+                     double* dS_dkappa, bt_stats* stats);
 
 /* Tangent-linear FP64 run: the signal and its derivative with respect to one
  * coefficient, param = BT_PARAM_D (D of region i), BT_PARAM_INVT2 (1/T2 of
@@ -254,8 +286,9 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *                           many times above the smallest it reached in the sweep (default 1e4)
  *   "mixed.reduce"          grid sums: 0 the last block to arrive sums and publishes, 1 every block sums
  *                           all partials itself, -1 by size (default; same bits either way)
- *   "mixed.extrapolate"     initial guess of each step: 2 = 3u_n - 3u_{n-1} + u_{n-2} (default),
- *                           1 = 2u_n - u_{n-1}, 0 = u_n
+ *   "mixed.extrapolate"     order of the initial guess of each step, extrapolated in time from the
+ *                           last states: 4 (default), 3, 2 (3u_n - 3u_{n-1} + u_{n-2}),
+ *                           1 (2u_n - u_{n-1}) or 0 (u_n)
  *   "mixed.inner_reductions" grid-wide reductions per inner COCG iteration: 1 (the
  *                           single-reduction rearrangement) or 2 (default, the textbook form); the
  *                           adjoint's and the pseudo-periodic launches always use 2

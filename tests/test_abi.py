@@ -35,6 +35,8 @@ def test_null_arguments_are_rejected(lib):
     assert lib.bt_periodic_info(None, None) == 1
     assert lib.bt_set_schedule_phase(None, None, 1, 1) == 1
     assert lib.bt_adjoint_batch(None, 1, None, None, None, 1e-9, 10, 0, None, None, None, None, None) == 1
+    assert lib.bt_adjoint_multi(None, 1, None, None, None, None, 1e-9, 10, 0, None, None, None, None, None) == 1
+    assert lib.bt_set_kappa_mode(None, 1) == 1
 
 
 def test_no_cpu_fallback_without_library(pkg, tmp_path, monkeypatch):

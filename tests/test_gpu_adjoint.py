@@ -192,3 +192,39 @@ def test_batched_autograd_and_16_cubed_layers(pkg, lib):
     for i in range(6):
         assert abs(float(s[i]) - refs[i]["signal"] / S0) <= 1e-6 * abs(refs[i]["signal"] / S0) + 1e-7
     ctx.close()
+
+
+def test_multi_mesh_adjoint_matches_fp64(pkg, lib):
+    """bt_adjoint_multi on a scaled-down uneven batch (seeded cylinder boxes of
+    6^3 ... 12^3 cubes sharing launches, plus one 28^3 box that runs alone):
+    every signal's gradients within 1e-5 of their scale of the FP64 adjoint of
+    that signal on its own mesh, signals within 1e-6."""
+    meshes = pkg.meshgen.uneven_meshes(count=4, seed=3, nmin=6, nmax=12, cube=1.5)
+    meshes.append(pkg.meshgen.uneven_meshes(count=1, seed=4, nmin=28, nmax=28, cube=1.0)[0])
+    p = pkg.sequences.pgse(10600, 43100)
+    fn, fo = pkg.sequences.profile_samples(p, 200.0)
+    ctxs, qs, gs = [], [], []
+    dirs = pkg.meshgen.fibonacci_directions(3)
+    for m in meshes:
+        c = pkg.Context(0)
+        c.mesh_upload(m["xyz"], m["tets"], m["region"], 2)
+        c.set_coefficients(m["D"], None, m["kappa"])
+        c.assemble()
+        c.set_schedule(fn, fo, 200.0)
+        ctxs.append(c)
+        qs.append([pkg.sequences.b_to_q(b, p.int4gb()) for b in (1000.0, 2500.0, 4000.0)])
+        gs.append(dirs)
+    out = pkg.adjoint_multi(ctxs, qs, gs, rtol=1e-9)
+    for k, c in enumerate(ctxs):
+        for i in range(3):
+            ref = c.adjoint(qs[k][i], gs[k][i], rtol=1e-13, max_iterations=20000)
+            assert abs(out["signal"][k][i] - ref["signal"]) <= 1e-6 * abs(ref["signal"]), (k, i)
+            for key in ("dD", "dinvT2", "dkappa"):
+                scale = np.max(np.abs(ref[key]))
+                if scale == 0.0:
+                    assert np.all(out[key][k][i] == 0.0), (k, i, key)
+                    continue
+                err = np.max(np.abs(out[key][k][i] - ref[key]))
+                assert err <= 1e-5 * scale, (k, i, key, err / scale)
+    for c in ctxs:
+        c.close()

@@ -271,3 +271,40 @@ def test_errors_are_status_codes(pkg, lib):
     out = ctx.solve([0.0], [1, 0, 0], rtol=1e-12)     # the context is still usable
     assert abs(out["signal"][0] / out["S0"] - 1.0) < 1e-12
     ctx.close()
+
+
+@pytest.mark.parametrize("case", ["layers", "cylinder"])
+def test_crouzeix_raviart_kappa(pkg, lib, case):
+    """The per-interface permeability as a Crouzeix-Raviart field (linear on a
+    facet whose cell has another interface facet): the interface matrix
+    entrywise and an FP64 signal against the oracle's CR mode, and a measurable
+    difference from the one-value-per-facet mode on the staircase mesh."""
+    if case == "layers":
+        xyz, tets, reg, D, iT2, kp = layered(pkg, n=8)
+        nr = 4
+    else:
+        xyz, tets = pkg.meshgen.kuhn_box(-6, 6, 10)
+        reg = pkg.meshgen.cylinder_regions(xyz, tets, [(0.3, -0.2)], [3.6])
+        D, iT2, kp, nr = np.array([3e-3, 2e-3]), np.zeros(2), np.array([[0.0, 4e-5], [4e-5, 0.0]]), 2
+    ctx = make_ctx(pkg, xyz, tets, reg, nr, D, iT2, kp)
+    ctx.set_kappa_mode("cr")
+    ctx.assemble()
+    sd = oracle.duplicated_system(xyz, tets, reg, D, iT2, kp, kappa_mode="cr")
+    A = gpu_csr(ctx, ctx.matrix("R"))
+    assert abs(A - sd["R"]).max() <= MAT_RTOL * abs(sd["R"]).max()
+    p = pkg.sequences.pgse(10600, 43100)
+    fn, fo = pkg.sequences.profile_samples(p, 200.0)
+    ctx.set_schedule(fn, fo, 200.0)
+    q = pkg.sequences.b_to_q(3000.0, p.int4gb())
+    g = np.array([0.6, 0.8, 0.0])
+    got = ctx.solve([q], [g], precision=pkg.PRECISION_FP64, rtol=1e-13, max_iterations=20000)
+    ref = oracle.solve_duplicated(sd, oracle.PGSE(10600, 43100), q, g, 200.0)
+    n_cr = got["signal"][0] / got["S0"]
+    assert abs(n_cr - ref.normalized) <= SIG_RTOL * abs(ref.normalized), (n_cr, ref.normalized)
+    with pytest.raises(pkg.BtError):
+        ctx.adjoint(q, g)
+    ctx.set_kappa_mode("facet")
+    ctx.assemble()
+    n_f = ctx.solve([q], [g], precision=pkg.PRECISION_FP64, rtol=1e-13)["signal"][0] / got["S0"]
+    assert abs(n_f - n_cr) > 1e-7 * abs(n_cr)
+    ctx.close()
