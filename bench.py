@@ -30,7 +30,10 @@ Legs (each its own timed region, named workload, precision and error):
 * ``uneven``: 16 small meshes of uneven size in one persistent launch
   (bt_solve_multi) against one launch per mesh;
 * ``adjoint``: batched mixed-precision gradients on the 48^3 layered sphere
-  against the FP64 adjoint.
+  against the FP64 adjoint;
+* ``cfg5`` (``--cfg5 128``, off by default: several minutes): the uneven batch
+  of 16 meshes of 24^3 ... 96^3 cubes, 2,048 signals, forward (bt_solve_multi)
+  and gradients (bt_adjoint_multi).
 
 ``--impl reference`` times the CPU restatement of the reference's solve path
 (two-field real system, Jacobi-BiCGSTAB rtol 1e-9 as GCloudDmriSolver.py ships
@@ -92,14 +95,15 @@ def alg_bytes_mixed(n, nnz, nsig, steps, iters, sweeps):
     16 + p,q out 16 + p,q,d,r in 32 + d,r,z out 24) = 192 B, plus the matrix
     nnz*(4 + 16) once per iteration for the whole batch.  Per time step and
     signal-dof: residual at u_n (gather u 16, r out 16) + extrapolated-guess
-    correction (gather two history vectors 16, r in/out 32, u in 8, history out
-    8, restart of the five slot vectors 80) = 176 B, matrix nnz*(4 + 8 + 32) +
-    nnz*(4 + 32).  Per refinement sweep and signal-dof: gather d 16, u and r
-    in/out as double-float 64, history in/out 16, restart 80 = 176 B, matrix
+    correction (gather the offset 8, r in/out 32, u in 8, correction out 8,
+    backward-difference table in 24 / out 24, restart of the five slot vectors
+    80) = 216 B, matrix nnz*(4 + 8 + 32) + nnz*(4 + 32).  Per refinement sweep
+    and signal-dof: gather d 16, u and r in/out as double-float 64, correction
+    in/out 16, table in 24, next offset out 8, restart 80 = 208 B, matrix
     nnz*(4 + 32).
     """
-    return (iters * (192 * n * nsig + 20 * nnz) + sweeps * (176 * n * nsig + 36 * nnz)
-            + steps * (176 * n * nsig + 80 * nnz))
+    return (iters * (192 * n * nsig + 20 * nnz) + sweeps * (208 * n * nsig + 36 * nnz)
+            + steps * (216 * n * nsig + 80 * nnz))
 
 
 class ClockSampler:
@@ -382,7 +386,7 @@ def gpu_run(args):
 
     if world == 1:
         stream_legs = (("batched", batched_leg, args.batched_signals), ("uneven", uneven_leg, args.uneven_meshes),
-                       ("adjoint", adjoint_leg, args.adjoint_signals))
+                       ("adjoint", adjoint_leg, args.adjoint_signals), ("cfg5", cfg5_leg, args.cfg5))
         for key, fnc, n in stream_legs:
             if n > 0:
                 legs[key] = fnc(args, pkg, stream, flush, peak, peak_src, traffic)
@@ -592,6 +596,73 @@ def uneven_leg(args, pkg, stream, flush, peak, peak_src, traffic):
             "max_rel_err_vs_fp64_largest_mesh": err}
 
 
+def cfg5_leg(args, pkg, stream, flush, peak, peak_src, traffic):
+    """The uneven batch: 16 seeded boxes of 24^3 ... 96^3 Kuhn cubes of 0.5 um
+    (edge counts stepped evenly) with random non-overlapping z-cylinders (radii
+    U[1.5,5] um up to an area fraction U[0.1,0.4]), kappa U[1e-5,1e-4], D_in 2e-3,
+    D_out 3e-3; `cfg5` signals per mesh from 32 Fibonacci directions x b in
+    {1000, 2000, 3000, 4000} (128: the whole 2,048-signal workload), PGSE.  Times
+    the forward solve of every mesh (bt_solve_multi) and the gradients dS/dD,
+    dS/d(1/T2), dS/dkappa of every signal (bt_adjoint_multi), and checks one
+    signal of every mesh against the FP64 path and the gradients of four meshes
+    against the FP64 adjoint."""
+    meshes = pkg.meshgen.uneven_meshes(count=16, seed=0, nmin=24, nmax=96, cube=0.5)
+    p = pkg.sequences.pgse(10600, 43100)
+    fn, fo = pkg.sequences.profile_samples(p, 200.0)
+    dirs = pkg.meshgen.fibonacci_directions(32)
+    allsig = [(b, d) for d in dirs for b in (1000.0, 2000.0, 3000.0, 4000.0)]
+    pick = np.linspace(0, len(allsig) - 1, min(args.cfg5, len(allsig))).astype(int)
+    qs = [pkg.sequences.b_to_q(allsig[i][0], p.int4gb()) for i in pick]
+    gs = [allsig[i][1] for i in pick]
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    ctxs = []
+    for m in meshes:
+        c = pkg.Context(local)
+        c.set_stream(stream.cuda_stream)
+        c.mesh_upload(m["xyz"], m["tets"], m["region"], 2)
+        c.set_coefficients(m["D"], None, m["kappa"])
+        c.assemble()
+        c.set_schedule(fn[:4], fo[:4], 200.0)
+        ctxs.append(c)
+    n = len(ctxs)
+    pkg.solve_multi(ctxs, [qs] * n, [gs] * n, rtol=1e-9)            # warm-up: the autotuner's trials
+    for c in ctxs:
+        c.set_schedule(fn, fo, 200.0)
+    timed = _event_timer(stream, flush)
+    ms_f, fw = timed(lambda: pkg.solve_multi(ctxs, [qs] * n, [gs] * n, rtol=1e-9))
+    ms_a, ad = timed(lambda: pkg.adjoint_multi(ctxs, [qs] * n, [gs] * n, rtol=1e-9))
+    nsig = n * len(qs)
+    err_f, err_a = [], []
+    for k, c in enumerate(ctxs):
+        i = (5 * k) % len(qs)
+        r64 = c.solve([qs[i]], [gs[i]], precision=pkg.PRECISION_FP64, rtol=1e-12, max_iterations=20000)["signal"][0]
+        err_f.append(float(abs(fw["signal"][k][i] - r64) / abs(r64)))
+        err_a.append(float(abs(ad["signal"][k][i] - r64) / abs(r64)))
+    gerr = {}
+    for k in (0, 5, 10, 15):
+        c = ctxs[k]
+        i = (5 * k) % len(qs)
+        ref = c.adjoint(qs[i], gs[i], rtol=1e-12, max_iterations=20000)
+        for key in ("dD", "dinvT2", "dkappa"):
+            e = float(np.max(np.abs(ad[key][k][i] - ref[key])) / np.max(np.abs(ref[key])))
+            gerr[key] = max(gerr.get(key, 0.0), e)
+    dofs = [c.info()["n_dofs"] for c in ctxs]
+    cells = [c.info()["n_cells"] for c in ctxs]
+    for c in ctxs:
+        c.close()
+    return {"workload": "cfg5: 16 seeded cylinder boxes, %d^3..%d^3 Kuhn cubes of 0.5 um (%d..%d dofs, up to %d "
+                        "tets), kappa U[1e-5,1e-4], D_in 2e-3 / D_out 3e-3, %d signals per mesh (32 Fibonacci "
+                        "directions x b 1000..4000), PGSE 10600/43100 us, dt 200 us"
+                        % (meshes[0]["n"], meshes[-1]["n"], min(dofs), max(dofs), max(cells), len(qs)),
+            "precision": "mixed", "signals": nsig, "dofs_per_mesh": dofs,
+            "forward": {"value": nsig / (ms_f / 1e3), "unit": "signals/s", "ms": ms_f,
+                        "max_rel_err_vs_fp64_one_signal_per_mesh": max(err_f)},
+            "gradients": {"value": nsig / (ms_a / 1e3), "unit": "gradients/s", "ms": ms_a,
+                          "parameters_per_signal": "D x2, 1/T2 x2, kappa x1",
+                          "signal_rel_err_vs_fp64": max(err_a),
+                          "max_rel_err_vs_fp64_adjoint_meshes_0_5_10_15": gerr}}
+
+
 def batched_profile(args):
     """One short launch for a profiler: `profile_signals` signals of the
     eight-cylinder 64^3 workload, schedule cut to `batched_profile` steps inside
@@ -658,6 +729,9 @@ def main():
                     help="signals of the batched-adjoint leg on the 48^3 layered sphere (0: skip)")
     ap.add_argument("--uneven-meshes", type=int, default=16,
                     help="meshes of the uneven multi-mesh leg (0: skip)")
+    ap.add_argument("--cfg5", type=int, default=0,
+                    help="signals per mesh of the 16-mesh 24^3..96^3 forward + adjoint leg (128: the whole "
+                         "workload, several minutes; 0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     args.ref_steps = max(1, min(args.steps, 2))
