@@ -34,7 +34,7 @@ EXPORTS = [
     "bt_get_dofs", "bt_get_colouring", "bt_get_solution", "bt_get_iterations", "bt_set_option",
     "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
     "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info", "bt_adjoint_batch", "bt_adjoint_multi",
-    "bt_set_kappa_mode",
+    "bt_set_kappa_mode", "bt_set_schedule_integral", "bt_set_periodic_mode", "bt_strong_periodic_info",
 ]
 
 
@@ -119,6 +119,10 @@ def load(path=None):
                                      _D, _D, C.POINTER(Stats)]),
         "bt_set_schedule_phase": (C.c_int, [_P, _D, C.c_int32, C.c_int32]),
         "bt_set_periodic": (C.c_int, [_P, _I32]),
+        "bt_set_schedule_integral": (C.c_int, [_P, _D, _D, C.c_int32, C.c_int32]),
+        "bt_set_periodic_mode": (C.c_int, [_P, C.c_int32]),
+        "bt_strong_periodic_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                              C.POINTER(C.c_int64)]),
         "bt_periodic_info": (C.c_int, [_P, C.POINTER(PeriodicInfo)]),
         "bt_adjoint_batch": (C.c_int, [_P, C.c_int32, _D, _D, _I32, C.c_double, C.c_int32, C.c_int32,
                                        _D, _D, _D, _D, C.POINTER(Stats)]),
@@ -242,9 +246,30 @@ class Context:
         Fo = np.ascontiguousarray(np.atleast_2d(np.asarray(F_old, np.float64)))
         self._check(self.lib.bt_set_schedule_phase(self.h, _dp(Fo), Fo.shape[1], Fo.shape[0]))
 
+    def set_schedule_integral(self, F_new, F_old):
+        """ift = int_0^t f at the implicit (F_new) and explicit (F_old) level of
+        every step, [n_sequences][n_steps]: the strong pseudo-periodic form's
+        schedule (also the weak form's phase)."""
+        Fn = np.ascontiguousarray(np.atleast_2d(np.asarray(F_new, np.float64)))
+        Fo = np.ascontiguousarray(np.atleast_2d(np.asarray(F_old, np.float64)))
+        if Fn.shape != Fo.shape:
+            raise ValueError("F_new and F_old must have the same shape")
+        self._check(self.lib.bt_set_schedule_integral(self.h, _dp(Fn), _dp(Fo), Fn.shape[1], Fn.shape[0]))
+
+    def set_periodic_mode(self, mode):
+        """'weak' (IsDomainPeriodic = False, the default) or 'strong'
+        (IsDomainPeriodic = True: constrained periodic space, FP64 BiCGSTAB)."""
+        self._check(self.lib.bt_set_periodic_mode(self.h, {"weak": 0, "strong": 1}[mode]))
+
+    def strong_periodic_info(self):
+        n, nnz, ncl = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        self._check(self.lib.bt_strong_periodic_info(self.h, C.byref(n), C.byref(nnz), C.byref(ncl)))
+        return {"n_dofs": n.value, "nnz": nnz.value, "n_classes": ncl.value}
+
     def set_periodic(self, periodic_dir):
-        """Weak pseudo-periodic boundaries along the axes with periodic_dir[d] = 1
-        (None or [0, 0, 0] switches them off)."""
+        """Pseudo-periodic boundaries along the axes with periodic_dir[d] = 1 in
+        the form set_periodic_mode selected (weak by default; None or [0, 0, 0]
+        switches them off)."""
         d = None if periodic_dir is None else np.ascontiguousarray(np.asarray(periodic_dir, np.int32).reshape(3))
         self._check(self.lib.bt_set_periodic(self.h, None if d is None else d.ctypes.data_as(_I32)))
 

@@ -20,10 +20,10 @@ Names, attributes and call order follow the reference's Python API
 The DOLFIN ``Mesh`` is replaced by :class:`Mesh` (vertex coordinates, tets and
 optional cell markers).  The linear solver argument is any object with a
 ``parameters`` mapping (e.g. :class:`KrylovSolver`); ``relative_tolerance`` and
-``maximum_iterations`` map to the COCG stopping rule.  Pseudo-periodic
-boundaries (``PeriodicDir != [0,0,0]``) are imposed weakly, as the reference
-does when ``IsDomainPeriodic`` is False; the strong form (``IsDomainPeriodic =
-True``, a constrained periodic function space) raises.
+``maximum_iterations`` map to the Krylov stopping rule.  Pseudo-periodic
+boundaries (``PeriodicDir != [0,0,0]``) are imposed weakly when
+``IsDomainPeriodic`` is False and strongly (constrained periodic function space,
+FP64 BiCGSTAB; the mesh must be periodic) when it is True, as in the reference.
 """
 
 import math
@@ -305,9 +305,6 @@ class MyDomain:
         self.D = "tensor"
 
     def Apply(self):
-        if sum(self.PeriodicDir) > 0 and self.IsDomainPeriodic:
-            raise NotImplementedError("strong pseudo-periodic boundaries (IsDomainPeriodic = True) are not "
-                                      "provided; the weak form (IsDomainPeriodic = False) is")
         self._ctx = None
 
     # -- internal -----------------------------------------------------------
@@ -355,11 +352,11 @@ class MyDomain:
             self._state = None
             self._periodic = None
         pdir = tuple(int(bool(d)) for d in self.PeriodicDir)
-        if sum(pdir) > 0 and self.IsDomainPeriodic:
-            raise NotImplementedError("strong pseudo-periodic boundaries (IsDomainPeriodic = True) are not provided")
-        if self._periodic != pdir:
+        mode = "strong" if (self.IsDomainPeriodic and sum(pdir) > 0) else "weak"
+        if self._periodic != (pdir, mode):
+            self._ctx.set_periodic_mode(mode)
             self._ctx.set_periodic(pdir)
-            self._periodic = pdir
+            self._periodic = (pdir, mode)
         if self._state != key:
             self._ctx.set_coefficients(Dr, iT2, kp)
             self._ctx.set_cell_diffusion(self._D_cell)
@@ -388,7 +385,7 @@ class MRI_simulation:
         fn, fo = seqs.profile_samples(mri_para.profile, self.k, self.loop)
         ctx.set_schedule(fn, fo, self.k, self.theta)
         if sum(mydomain.PeriodicDir) > 0:
-            ctx.set_schedule_phase(seqs.phase_samples(mri_para.profile, self.k, self.loop))
+            ctx.set_schedule_integral(*seqs.integral_samples(mri_para.profile, self.k, self.loop))
         params = getattr(linsolver, "parameters", {}) if linsolver is not None else {}
         rtol = float(params.get("relative_tolerance", 1e-12))
         maxit = int(params.get("maximum_iterations", 2000))
@@ -437,7 +434,8 @@ def simulate(mydomain, profiles, bvalues, gdirs, profile_index=None, k=200.0, th
     ctx = mydomain.context(para)
     ctx.set_schedule(np.array(fns), np.array(fos), k, theta)
     if sum(mydomain.PeriodicDir) > 0:
-        ctx.set_schedule_phase(np.array([seqs.phase_samples(p, k, loop) for p in profiles]))
+        Fs = [seqs.integral_samples(p, k, loop) for p in profiles]
+        ctx.set_schedule_integral(np.array([f[0] for f in Fs]), np.array([f[1] for f in Fs]))
     prec = _native.PRECISION_MIXED if precision == "mixed" else _native.PRECISION_FP64
     if rtol is None:
         rtol = 1e-12 if prec == _native.PRECISION_FP64 else 1e-9

@@ -82,6 +82,7 @@ int bt_destroy(bt_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     bt::free_solver64(ctx);
     bt::free_solver_mixed(ctx);
+    bt::free_strong(ctx);
     ctx->mesh = bt::Mesh();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -117,6 +118,8 @@ int bt_mesh_upload(bt_ctx* ctx, const double* xyz, int64_t n_vertices, const int
         ctx->mat.done = false;
         ctx->coeffs = bt::Coeffs();
         ctx->per = bt::Periodic();
+        ctx->periodic_mode = BT_PERIODIC_WEAK;
+        bt::free_strong(ctx);
         bt::free_solver64(ctx);
         bt::free_solver_mixed(ctx);
         bt::build_graph(ctx, xyz, n_vertices, tets, n_cells, cell_region, n_regions, region_compartment);
@@ -256,6 +259,7 @@ int bt_set_schedule(bt_ctx* ctx, const double* f_new, const double* f_old, int32
         S.theta = theta;
         S.set = true;
         S.F_old.clear();
+        S.F_new.clear();
         S.phase_set = false;
     });
 }
@@ -276,15 +280,67 @@ int bt_set_schedule_phase(bt_ctx* ctx, const double* F_old, int32_t n_steps, int
     });
 }
 
+int bt_set_schedule_integral(bt_ctx* ctx, const double* F_new, const double* F_old, int32_t n_steps,
+                             int32_t n_sequences) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        bt::Schedule& S = ctx->sched;
+        BT_REQUIRE(S.set, BT_ERR_STATE, "bt_set_schedule_integral: call bt_set_schedule first");
+        BT_REQUIRE(F_new && F_old, BT_ERR_INVALID, "bt_set_schedule_integral: NULL array");
+        BT_REQUIRE(n_steps == S.n_steps && n_sequences == S.n_seq, BT_ERR_INVALID,
+                   "bt_set_schedule_integral: sizes differ from the schedule");
+        const size_t n = (size_t)n_steps * n_sequences;
+        for (size_t i = 0; i < n; ++i)
+            BT_REQUIRE(std::isfinite(F_new[i]) && std::isfinite(F_old[i]), BT_ERR_INVALID,
+                       "bt_set_schedule_integral: values must be finite");
+        S.F_new.assign(F_new, F_new + n);
+        S.F_old.assign(F_old, F_old + n);
+        S.phase_set = true;
+    });
+}
+
+// The directions last given to bt_set_periodic (weak or strong form).
+static void apply_periodic(bt_ctx* ctx, const int32_t* dir) {
+    const int32_t off[3] = {0, 0, 0};
+    bt::free_solver_mixed(ctx);   // cached tuning and packed matrices do not hold the boundary term
+    if (ctx->periodic_mode == BT_PERIODIC_STRONG) {
+        bt::set_periodic(ctx, off);
+        bt::set_strong(ctx, dir);
+    } else {
+        bt::free_strong(ctx);
+        bt::set_periodic(ctx, dir);
+    }
+}
+
 int bt_set_periodic(bt_ctx* ctx, const int32_t* periodic_dir) {
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built, BT_ERR_STATE, "bt_set_periodic: no mesh");
         const int32_t off[3] = {0, 0, 0};
         use_device(ctx);
-        bt::free_solver_mixed(ctx);   // cached tuning and packed matrices do not hold the boundary term
-        bt::set_periodic(ctx, periodic_dir ? periodic_dir : off);
+        apply_periodic(ctx, periodic_dir ? periodic_dir : off);
     });
+}
+
+int bt_set_periodic_mode(bt_ctx* ctx, int32_t mode) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(mode == BT_PERIODIC_WEAK || mode == BT_PERIODIC_STRONG, BT_ERR_INVALID,
+                   "bt_set_periodic_mode: mode must be BT_PERIODIC_WEAK or BT_PERIODIC_STRONG");
+        BT_REQUIRE(ctx->mesh.built, BT_ERR_STATE, "bt_set_periodic_mode: no mesh");
+        use_device(ctx);
+        int32_t dir[3] = {0, 0, 0};
+        for (int d = 0; d < 3; ++d)
+            dir[d] = ctx->per.dir[d];
+        if (ctx->periodic_mode == BT_PERIODIC_STRONG) bt::strong_directions(ctx, dir);
+        ctx->periodic_mode = mode;
+        apply_periodic(ctx, dir);
+    });
+}
+
+int bt_strong_periodic_info(bt_ctx* ctx, int64_t* n_dofs, int64_t* nnz, int64_t* n_classes) {
+    if (!ctx || !n_dofs || !nnz || !n_classes) return BT_ERR_INVALID;
+    return guarded(ctx, [&] { bt::strong_info(ctx, n_dofs, nnz, n_classes); });
 }
 
 int bt_periodic_info(bt_ctx* ctx, bt_periodic_info_t* out) {
@@ -323,7 +379,14 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
                 BT_REQUIRE(std::isfinite(u0[v]), BT_ERR_INVALID, "bt_solve: u0 must be finite");
         use_device(ctx);
         ctx->last_precision = -1;
-        if (precision == BT_PRECISION_FP64) {
+        ctx->last_strong = false;
+        if (bt::strong_active(ctx)) {
+            BT_REQUIRE(precision == BT_PRECISION_FP64, BT_ERR_INVALID,
+                       "bt_solve: the strong pseudo-periodic form runs on the FP64 path only");
+            bt::solve_strong(ctx, n_signals, q, gdir, sequence, u0, rtol, max_iterations, signal_out,
+                             compartment_out, stats);
+            ctx->last_strong = true;
+        } else if (precision == BT_PRECISION_FP64) {
             bt::solve_fp64(ctx, n_signals, q, gdir, sequence, u0, rtol, max_iterations, signal_out,
                            compartment_out, stats);
         } else if (precision == BT_PRECISION_MIXED) {
@@ -366,6 +429,8 @@ int bt_solve_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_s
                        "bt_solve_multi: every mesh needs bt_assemble and bt_set_schedule");
             BT_REQUIRE(n_signals[m] >= 1 && n_signals[m] <= 256, BT_ERR_INVALID,
                        "bt_solve_multi: 1..256 signals per mesh");
+            BT_REQUIRE(!bt::strong_active(c), BT_ERR_STATE,
+                       "bt_solve_multi: the strong pseudo-periodic form runs on the FP64 path (bt_solve) only");
             total += n_signals[m];
         }
         for (int64_t i = 0; i < total; ++i) {
@@ -397,6 +462,7 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_tangent: mesh not assembled");
+        BT_REQUIRE(!bt::strong_active(ctx), BT_ERR_STATE, "bt_tangent: not defined with the strong pseudo-periodic form");
         BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_tangent: no schedule");
         BT_REQUIRE(gdir && signal_out && dsignal_out, BT_ERR_INVALID, "bt_tangent: bad arguments");
         BT_REQUIRE(std::isfinite(q) && std::isfinite(gdir[0]) && std::isfinite(gdir[1]) && std::isfinite(gdir[2]),
@@ -417,6 +483,7 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint: mesh not assembled");
+        BT_REQUIRE(!bt::strong_active(ctx), BT_ERR_STATE, "bt_adjoint: not defined with the strong pseudo-periodic form");
         BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_adjoint: no schedule");
         BT_REQUIRE(gdir && signal_out, BT_ERR_INVALID, "bt_adjoint: bad arguments");
         BT_REQUIRE(std::isfinite(q) && std::isfinite(gdir[0]) && std::isfinite(gdir[1]) && std::isfinite(gdir[2]),
@@ -439,6 +506,8 @@ int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const doub
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint_batch: mesh not assembled");
+        BT_REQUIRE(!bt::strong_active(ctx), BT_ERR_STATE,
+                   "bt_adjoint_batch: not defined with the strong pseudo-periodic form");
         BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_adjoint_batch: no schedule");
         BT_REQUIRE(n_signals >= 1 && q && gdir && signal_out, BT_ERR_INVALID, "bt_adjoint_batch: bad arguments");
         BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
@@ -476,6 +545,8 @@ int bt_adjoint_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n
                        "bt_adjoint_multi: every mesh needs bt_assemble and bt_set_schedule");
             BT_REQUIRE(n_signals[m] >= 1 && n_signals[m] <= 256, BT_ERR_INVALID,
                        "bt_adjoint_multi: 1..256 signals per mesh");
+            BT_REQUIRE(!bt::strong_active(c), BT_ERR_STATE,
+                       "bt_adjoint_multi: not defined with the strong pseudo-periodic form");
             total += n_signals[m];
         }
         for (int64_t i = 0; i < total; ++i) {
@@ -612,7 +683,9 @@ int bt_get_solution(bt_ctx* ctx, int32_t index, double* u) {
         BT_REQUIRE(u, BT_ERR_INVALID, "bt_get_solution: NULL output");
         use_device(ctx);
         BT_REQUIRE(ctx->last_precision >= 0, BT_ERR_STATE, "bt_get_solution: no solve yet");
-        if (ctx->last_precision == BT_PRECISION_MIXED)
+        if (ctx->last_strong)
+            bt::get_solution_strong(ctx, index, u);
+        else if (ctx->last_precision == BT_PRECISION_MIXED)
             bt::get_solution_mixed(ctx, index, u);
         else
             bt::get_solution_fp64(ctx, index, u);

@@ -357,6 +357,7 @@ void assemble_all(bt_ctx* ctx) {
     BT_REQUIRE(st == DEV_OK, BT_ERR_INVALID, "bt_assemble: a cell coupling is missing from the graph");
     m.volume = device_sum(A.vw, m.n_v, s);
     A.done = true;
+    ++A.version;
 }
 
 }  // namespace bt

@@ -99,6 +99,7 @@ constexpr int kMaxColours = 256;
 // ------------------------------------------------------------- the context ----
 struct Solver64;     // FP64 persistent stepper workspace (stepper64.cu)
 struct SolverMixed;  // batched mixed-precision workspace (batched.cu)
+struct Strong;       // strong pseudo-periodic form: folded system and stepper (strong.cu)
 
 struct Mesh {
     int64_t n_v = 0, n_t = 0;
@@ -140,11 +141,13 @@ struct Assembled {
     DevBuf<double> w;                       // signal weight per dof
     DevBuf<double> vw;                      // int phi_v over the whole mesh, per vertex
     bool done = false;
+    int64_t version = 0;                    // incremented by every assembly
 };
 
 struct Schedule {
     std::vector<double> f_new, f_old;  // [n_seq * n_steps]
     std::vector<double> F_old;         // integral F = int_0^t f at the explicit level (pseudo-periodic phase)
+    std::vector<double> F_new;         // F at the implicit level (strong pseudo-periodic form)
     int32_t n_steps = 0, n_seq = 0;
     double dt = 0.0, theta = 0.5;
     bool set = false;
@@ -188,6 +191,9 @@ struct bt_ctx {
     bt::Periodic per;
     bt::Solver64* s64 = nullptr;
     bt::SolverMixed* smx = nullptr;
+    bt::Strong* strong = nullptr;
+    int periodic_mode = 0;            // BT_PERIODIC_WEAK or BT_PERIODIC_STRONG
+    bool last_strong = false;         // the last solve ran the strong pseudo-periodic stepper
     // last solve
     int32_t last_nsig = 0;
     int32_t last_precision = -1;
@@ -235,6 +241,14 @@ void solve_mixed_multi(bt_ctx* const* ctxs, int32_t n_meshes, const int32_t* nsi
                        bt_stats* st);
 void reset_tuning_mixed(bt_ctx* ctx);
 void set_periodic(bt_ctx* ctx, const int32_t* dir);
+void set_strong(bt_ctx* ctx, const int32_t* dir);
+bool strong_active(const bt_ctx* ctx);
+void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
+                  const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st);
+void get_solution_strong(bt_ctx* ctx, int32_t index, double* u);
+void strong_info(const bt_ctx* ctx, int64_t* n_dofs, int64_t* nnz, int64_t* n_classes);
+void free_strong(bt_ctx* ctx);
+void strong_directions(const bt_ctx* ctx, int32_t* dir);
 void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
                    int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
                    bt_stats* st);

@@ -232,6 +232,14 @@ def phase_samples(profile, k, loop="solve"):
     return np.array([profile.F(t) for t in to])
 
 
+def integral_samples(profile, k, loop="solve"):
+    """ift = int_0^t f at the implicit and explicit level of every step: the
+    ``itime_profile(t)`` and ``itime_profile(tp)`` of the strong pseudo-periodic
+    forms (``DmriFemLib.py:148-238, 897-905``)."""
+    tn, to = schedule(profile.T, k, loop)
+    return np.array([profile.F(t) for t in tn]), np.array([profile.F(t) for t in to])
+
+
 def b_to_q(bvalue, int4gb):
     """``convert_b2q`` (``DmriFemLib.py:840-842``)."""
     return math.sqrt(bvalue) / math.sqrt(int4gb)

@@ -168,6 +168,47 @@ int bt_set_schedule(bt_ctx* ctx, const double* f_new, const double* f_old,
  * it.  Needed only when periodic directions are set. */
 int bt_set_schedule_phase(bt_ctx* ctx, const double* F_old, int32_t n_steps, int32_t n_sequences);
 
+/* Integral schedule of the strong pseudo-periodic form: F_new[n_sequences*n_steps]
+ * = itime_profile(t) at the implicit level and F_old[...] = itime_profile(tp) at the
+ * explicit level of each step (the ift arguments of ThetaMethodF/L_sBC1c/2c,
+ * DmriFemLib.py:148-238, 897-905).  Also sets the weak form's phase schedule
+ * (F_old).  Sizes must equal the schedule's; bt_set_schedule clears it. */
+int bt_set_schedule_integral(bt_ctx* ctx, const double* F_new, const double* F_old, int32_t n_steps,
+                             int32_t n_sequences);
+
+/* Which pseudo-periodic form bt_set_periodic selects: BT_PERIODIC_WEAK (default,
+ * IsDomainPeriodic = False) or BT_PERIODIC_STRONG (IsDomainPeriodic = True: the
+ * constrained periodic space of MyFunctionSpaces with PeriodicBD,
+ * DmriFemLib.py:325-378, 453-486, and the forms ThetaMethodF/L_sBC1c/2c,
+ * DmriFemLib.py:148-238).  Applies to the directions already set and to later
+ * bt_set_periodic calls; bt_mesh_upload resets it to weak.
+ *
+ * Strong form: the mesh must be periodic (every vertex of a max face has a
+ * vertex at its image on the min face, within 1e-6 hmin) with periodic
+ * compartments (a folded vertex touches the compartments of its image), at most
+ * two compartments.  Pairing follows the reference's PeriodicBD: a max-face
+ * vertex folds onto its image along the first periodic direction whose max face
+ * holds it, nothing is chained (with several directions the edge columns
+ * (xmax, ymin), (xmin, ymin) stay separate dofs, as in the reference).  Solved by
+ * a persistent FP64 Jacobi-BiCGSTAB stepper (the operator has first-order terms
+ * and is not complex symmetric) to ||r|| <= rtol ||b||; bt_solve needs
+ * BT_PRECISION_FP64 and bt_set_schedule_integral.  A signal whose gradient has a
+ * component along which (D g).n does not vanish on an exterior facet off the
+ * periodic faces that touches a compartment interface is refused
+ * (BT_ERR_INVALID): there the reference's phase-blind outer term acts on the
+ * other compartment's dead rows, which one dof per live (vertex, compartment)
+ * pair does not hold.  bt_get_solution returns the unfolded dofs (a folded dof's
+ * value on each of its vertices).  The adjoints, bt_tangent and the mixed path
+ * reject the strong form. */
+#define BT_PERIODIC_WEAK 0
+#define BT_PERIODIC_STRONG 1
+int bt_set_periodic_mode(bt_ctx* ctx, int32_t mode);
+
+/* Size of the folded system of the strong form after the last solve that set it
+ * up: dofs, stored entries and vertex classes (0 when the strong form is off or
+ * not set up yet). */
+int bt_strong_periodic_info(bt_ctx* ctx, int64_t* n_dofs, int64_t* nnz, int64_t* n_classes);
+
 /* Weak pseudo-periodic boundary conditions: periodic_dir[3] = mydomain.PeriodicDir
  * (0/1 per axis; all 0 or NULL switches them off), the reference's default
  * form when IsDomainPeriodic is False (ThetaMethodF/L_wBC1c/2c,
@@ -177,8 +218,9 @@ int bt_set_schedule_phase(bt_ctx* ctx, const double* F_old, int32_t n_steps, int
  * (1-theta) int kappa_e ubc v ds with ubc = u_n at the mirror point on the
  * opposite face times exp(i q F(tp) g.shift).  The box is the mesh's bounding
  * box; the mesh need not be periodic.  Call after bt_mesh_upload (a new mesh
- * clears it); the strong form (IsDomainPeriodic, a constrained periodic space)
- * is not provided.  bt_adjoint and bt_tangent reject a periodic context. */
+ * clears it).  With bt_set_periodic_mode(BT_PERIODIC_STRONG) the same call selects
+ * the strong form instead (see there).  bt_adjoint and bt_tangent reject a
+ * periodic context. */
 int bt_set_periodic(bt_ctx* ctx, const int32_t* periodic_dir);
 int bt_periodic_info(bt_ctx* ctx, bt_periodic_info_t* out);
 

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
+import oracle.strong  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
@@ -135,6 +136,9 @@ def test_reference_api(pkg, lib):
     reg = np.zeros(len(tets), np.int32)
     ref = oracle_signal(xyz, tets, reg, [2e-3], 0.0, [1, 0, 0], para.qvalue, [1, 0, 0], 50.0, 1000.0, 10000.0)
     assert abs(sim.signal - ref.signal) <= SIG_RTOL * abs(ref.signal)
+    # IsDomainPeriodic = True: the strong form (uniform solution of the homogeneous box)
     dom.IsDomainPeriodic = True
-    with pytest.raises(NotImplementedError):
-        dom.Apply()
+    dom.Apply()
+    sim.solve(dom, para)
+    exact = oracle.strong.uniform_box_signal(1000.0, 2e-3, 0.0, oracle.PGSE(1000.0, 10000.0), para.qvalue, 50.0)
+    assert abs(sim.signal - exact) <= SIG_RTOL * abs(exact)

@@ -1,0 +1,160 @@
+"""GPU: strong pseudo-periodic form (bt_set_periodic_mode(BT_PERIODIC_STRONG)) against
+the CPU oracle's folded complex system (FP64, 1e-9), the closed form of the
+homogeneous box, the reference-named API, and the refusals."""
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import strong
+
+pytestmark = pytest.mark.gpu
+
+SIG_RTOL = 1e-9
+DELTA, BIGDELTA, DT = 2000.0, 5000.0, 100.0
+
+
+def cube_cylinder_regions(xyz, tets, r):
+    """z-cylinder on whole Kuhn cubes (the staircase is the same on opposite faces)."""
+    X = xyz[tets]
+    c = 0.5 * (X.min(axis=1) + X.max(axis=1))
+    return (c[:, 0] ** 2 + c[:, 1] ** 2 < r * r).astype(np.int32)
+
+
+def strong_ctx(pkg, xyz, tets, reg, nr, D, iT2, kp, pdir, seq, dt=DT):
+    ctx = pkg.Context(0)
+    ctx.mesh_upload(xyz, tets, reg, nr)
+    ctx.set_coefficients(D, iT2, kp)
+    ctx.assemble()
+    ctx.set_periodic_mode("strong")
+    ctx.set_periodic(pdir)
+    fn, fo = pkg.sequences.profile_samples(seq, dt)
+    ctx.set_schedule(fn, fo, dt)
+    ctx.set_schedule_integral(*pkg.sequences.integral_samples(seq, dt))
+    return ctx
+
+
+def test_homogeneous_box_closed_form(pkg, lib):
+    xyz, tets = pkg.meshgen.kuhn_box(0.0, 6.0, 6)
+    reg = np.zeros(len(tets), np.int32)
+    seq = pkg.sequences.pgse(DELTA, BIGDELTA)
+    q = pkg.sequences.b_to_q(3000.0, seq.int4gb())
+    D, iT2 = 2e-3, 1.0 / 8e4
+    ctx = strong_ctx(pkg, xyz, tets, reg, 1, [D], [iT2], None, [1, 0, 0], seq)
+    out = ctx.solve([q], [1.0, 0.0, 0.0], rtol=1e-13, max_iterations=5000)
+    exact = strong.uniform_box_signal(216.0, D, iT2, oracle.PGSE(DELTA, BIGDELTA), q, DT)
+    assert abs(out["signal"][0] - exact) <= 1e-10 * abs(exact), (out["signal"][0], exact)
+    info = ctx.strong_periodic_info()
+    # 7^3 vertices, the x = 6 face folded onto x = 0
+    assert info["n_classes"] == 6 * 7 * 7 and info["n_dofs"] == 6 * 7 * 7
+    u = ctx.solution(0)
+    assert np.max(np.abs(u - u[0])) <= 1e-11 * abs(u[0])
+    ctx.close()
+
+
+@pytest.mark.parametrize("pdir,g", [([1, 1, 1], (1.0, 0.4, 0.3)), ([1, 1, 0], (0.6, 1.0, 0.0)),
+                                    ([0, 1, 0], (0.2, 1.0, 0.0))])
+def test_two_compartments_match_oracle(pkg, lib, pdir, g):
+    xyz, tets = pkg.meshgen.kuhn_box(-5.0, 5.0, 8)
+    reg = cube_cylinder_regions(xyz, tets, 2.6)
+    D = [3e-3, 1.5e-3]
+    iT2 = [0.0, 1.0 / 6e4]
+    kp = np.array([[0.0, 2e-5], [2e-5, 0.0]])
+    seq = pkg.sequences.pgse(DELTA, BIGDELTA)
+    g = np.asarray(g) / np.linalg.norm(g)
+    qs = [pkg.sequences.b_to_q(b, seq.int4gb()) for b in (1000.0, 2500.0)]
+    ctx = strong_ctx(pkg, xyz, tets, reg, 2, D, iT2, kp, pdir, seq)
+    out = ctx.solve(qs, np.tile(g, (2, 1)), rtol=1e-13, max_iterations=5000, compartments=True)
+    sd = strong.duplicated_strong(xyz, tets, reg, np.array(D), np.array(iT2), kp, pdir, g)
+    for i, q in enumerate(qs):
+        ref = strong.solve_strong(sd, oracle.PGSE(DELTA, BIGDELTA), q, DT)
+        assert abs(out["signal"][i] - ref["signal"]) <= SIG_RTOL * abs(ref["signal"]), (out["signal"][i], ref["signal"])
+        assert np.allclose(out["compartments"][i], ref["compartments"], rtol=1e-9, atol=1e-9 * abs(ref["signal"]))
+        assert len(ctx.solution(i)) == ctx.info()["n_dofs"]     # unfolded dofs
+    info = ctx.strong_periodic_info()
+    assert info["n_dofs"] == sd["n"]
+    ctx.close()
+
+
+def test_solution_on_unfolded_dofs(pkg, lib):
+    xyz, tets = pkg.meshgen.kuhn_box(-5.0, 5.0, 6)
+    reg = cube_cylinder_regions(xyz, tets, 2.6)
+    seq = pkg.sequences.pgse(DELTA, BIGDELTA)
+    q = pkg.sequences.b_to_q(2000.0, seq.int4gb())
+    g = np.array([0.8, 0.6, 0.0])
+    ctx = strong_ctx(pkg, xyz, tets, reg, 2, [3e-3, 3e-3], None, np.array([[0, 1e-5], [1e-5, 0]]), [1, 1, 1], seq)
+    ctx.solve([q], g, rtol=1e-13, max_iterations=5000)
+    u = ctx.solution(0)
+    sd = strong.duplicated_strong(xyz, tets, reg, 3e-3, 0.0, np.array([[0, 1e-5], [1e-5, 0]]), [1, 1, 1], g)
+    ref = strong.solve_strong(sd, oracle.PGSE(DELTA, BIGDELTA), q, DT)
+    # unfolded dof (vertex v, compartment c) -> oracle dof of (class of v, c)
+    plain = oracle.duplicated_system(xyz, tets, reg, 3e-3)
+    cls = sd["class_of_vertex"][plain["vertex"]]
+    od = sd["dof"][cls, plain["field"]]
+    assert np.all(od >= 0)
+    assert np.max(np.abs(u - ref["u"][od])) <= 1e-9 * np.max(np.abs(ref["u"]))
+    ctx.close()
+
+
+def test_refusals(pkg, lib):
+    xyz, tets = pkg.meshgen.kuhn_box(-5.0, 5.0, 6)
+    seq = pkg.sequences.pgse(DELTA, BIGDELTA)
+    q = pkg.sequences.b_to_q(1000.0, seq.int4gb())
+    # a gradient with a component normal to the non-periodic faces where the
+    # cylinder's interface meets them
+    reg = cube_cylinder_regions(xyz, tets, 2.6)
+    ctx = strong_ctx(pkg, xyz, tets, reg, 2, [3e-3, 3e-3], None, 1e-5, [1, 1, 0], seq)
+    with pytest.raises(RuntimeError, match="must vanish"):
+        ctx.solve([q], [0.3, 0.2, 1.0], rtol=1e-12, max_iterations=5000)
+    ctx.solve([q], [0.6, 0.8, 0.0], rtol=1e-12, max_iterations=5000)          # in-plane: accepted
+    with pytest.raises(RuntimeError, match="FP64"):
+        ctx.solve([q], [0.6, 0.8, 0.0], precision=pkg.PRECISION_MIXED, rtol=1e-9, max_iterations=5000)
+    with pytest.raises(RuntimeError, match="strong"):
+        ctx.adjoint(q, [0.6, 0.8, 0.0])
+    # weak mode again: the same directions, the penalty form
+    ctx.set_periodic_mode("weak")
+    assert ctx.periodic_info()["active"] == 1 and ctx.strong_periodic_info()["n_dofs"] == 0
+    ctx.close()
+    # compartments that differ across a periodic face (per-tetrahedron staircase)
+    reg2 = pkg.meshgen.cylinder_regions(xyz, tets, [(0.0, 0.0)], [2.6])
+    ctx = strong_ctx(pkg, xyz, tets, reg2, 2, [3e-3, 3e-3], None, 1e-5, [0, 0, 1], seq)
+    with pytest.raises(RuntimeError, match="not periodic"):
+        ctx.solve([q], [0.0, 0.0, 1.0], rtol=1e-12, max_iterations=5000)
+    ctx.close()
+    # a mesh whose max face has no matching vertices
+    xyz3 = xyz.copy()
+    on_max = np.isclose(xyz3[:, 0], 5.0) & ~np.isclose(xyz3[:, 1], -5.0) & ~np.isclose(xyz3[:, 1], 5.0)
+    xyz3[on_max, 1] += 0.3 * (10.0 / 6)
+    ctx = strong_ctx(pkg, xyz3, tets, np.zeros(len(tets), np.int32), 1, [3e-3], None, None, [1, 0, 0], seq)
+    with pytest.raises(RuntimeError, match="mesh not periodic"):
+        ctx.solve([q], [1.0, 0.0, 0.0], rtol=1e-12, max_iterations=5000)
+    ctx.close()
+
+
+def test_reference_api(pkg, lib):
+    xyz, tets = pkg.meshgen.kuhn_box(-5.0, 5.0, 6)
+    reg = cube_cylinder_regions(xyz, tets, 2.6)
+    mesh = pkg.Mesh(xyz, tets, reg)
+    para = pkg.MRI_parameters()
+    para.bvalue, para.delta, para.Delta = 2000.0, DELTA, BIGDELTA
+    para.set_gradient_dir(mesh, 1, 1, 0)
+    para.Apply()
+    dom = pkg.MyDomain(mesh, para)
+    dom.PeriodicDir = [1, 1, 1]
+    dom.IsDomainPeriodic = True
+    dom.IsDomainMultiple = True
+    dom.kappa = 1e-5
+    dom.Apply()
+    dom.D = 3e-3
+    sim = pkg.MRI_simulation()
+    sim.k = DT
+    s = sim.solve(dom, para)
+    g = np.array([1.0, 1.0, 0.0]) / np.sqrt(2.0)
+    sd = strong.duplicated_strong(xyz, tets, reg, 3e-3, 0.0, 1e-5, [1, 1, 1], g)
+    ref = strong.solve_strong(sd, oracle.PGSE(DELTA, BIGDELTA), para.qvalue, DT)
+    assert abs(s - ref["signal"]) <= SIG_RTOL * abs(ref["signal"])
+    # the weak form on the same domain gives another signal
+    dom.IsDomainPeriodic = False
+    dom.Apply()
+    w = sim.solve(dom, para)
+    assert abs(w - s) > 1e-6 * abs(s)

@@ -80,17 +80,22 @@ def test_sympy_profile_matches(pkg):
     assert para.time_profile(10600.0) == 0.0 and para.time_profile(200.0) == 1.0
 
 
-def test_strong_periodic_rejected(pkg):
-    """The weak pseudo-periodic form is accepted; the strong one (a constrained
-    periodic space, IsDomainPeriodic = True) is not provided."""
+def test_strong_periodic_accepted_and_integral_schedule(pkg):
+    """IsDomainPeriodic = True with PeriodicDir set selects the strong form
+    (Apply accepts it); its schedule is ift at both levels, with
+    F_new[s] = F_old[s + 1] (tp of a step is t of the one before)."""
     mesh = pkg.Mesh(*pkg.meshgen.kuhn_box(-1, 1, 2))
     para = pkg.MRI_parameters()
     dom = pkg.MyDomain(mesh, para)
     dom.PeriodicDir = [1, 0, 0]
-    dom.Apply()
     dom.IsDomainPeriodic = True
-    with pytest.raises(NotImplementedError):
-        dom.Apply()
+    dom.Apply()
+    p = pkg.sequences.pgse(1000.0, 3000.0)
+    Fn, Fo = pkg.sequences.integral_samples(p, 200.0)
+    assert len(Fn) == len(Fo) and np.allclose(Fn[:-1], Fo[1:])
+    # the reference's first solve has t = tp = 0 (DmriFemLib.py:889-905)
+    assert Fo[0] == 0.0 and Fn[0] == 0.0 and np.isclose(Fn[1], p.F(200.0))
+    assert np.allclose(Fo, pkg.sequences.phase_samples(p, 200.0))
 
 
 def test_phase_samples(pkg):
