@@ -386,7 +386,8 @@ def gpu_run(args):
 
     if world == 1:
         stream_legs = (("batched", batched_leg, args.batched_signals), ("uneven", uneven_leg, args.uneven_meshes),
-                       ("adjoint", adjoint_leg, args.adjoint_signals), ("cfg5", cfg5_leg, args.cfg5))
+                       ("adjoint", adjoint_leg, args.adjoint_signals), ("strong", strong_leg, args.strong_signals),
+                       ("cfg5", cfg5_leg, args.cfg5))
         for key, fnc, n in stream_legs:
             if n > 0:
                 legs[key] = fnc(args, pkg, stream, flush, peak, peak_src, traffic)
@@ -596,6 +597,51 @@ def uneven_leg(args, pkg, stream, flush, peak, peak_src, traffic):
             "max_rel_err_vs_fp64_largest_mesh": err}
 
 
+def strong_leg(args, pkg, stream, flush, peak, peak_src, traffic):
+    """Strong pseudo-periodic form (IsDomainPeriodic = True): the workload of
+    tests/golden/oracle_strong_signals.json (12^3 Kuhn box of 4/3 um cubes, a
+    z-cylinder on whole cubes, periodic in x, y, z, PGSE 10600/43100 us, 270
+    steps, 4 signals), FP64 Jacobi-BiCGSTAB stepper, each signal against the
+    oracle's value in that fixture."""
+    gold = load_json("tests", "golden", "oracle_strong_signals.json")
+    if gold is None:
+        return {"unavailable": "tests/golden/oracle_strong_signals.json missing"}
+    s = gold["setup"]
+    lo, hi = s["box"]
+    xyz, tets = pkg.meshgen.kuhn_box(lo, hi, s["cubes_per_axis"])
+    X = xyz[tets]
+    c = 0.5 * (X.min(axis=1) + X.max(axis=1))
+    reg = (c[:, 0] ** 2 + c[:, 1] ** 2 < s["radius"] ** 2).astype(np.int32)
+    p = pkg.sequences.pgse(s["delta"], s["Delta"])
+    fn, fo = pkg.sequences.profile_samples(p, s["dt"])
+    ctx = pkg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    ctx.set_stream(stream.cuda_stream)
+    ctx.mesh_upload(xyz, tets, reg, 2)
+    ctx.set_coefficients(s["D"], None, np.array([[0.0, s["kappa"]], [s["kappa"], 0.0]]))
+    ctx.assemble()
+    ctx.set_periodic_mode("strong")
+    ctx.set_periodic(s["periodic_dir"])
+    ctx.set_schedule(fn, fo, s["dt"])
+    ctx.set_schedule_integral(*pkg.sequences.integral_samples(p, s["dt"]))
+    sig = gold["signals"][:max(1, args.strong_signals)]
+    q = np.array([g["q"] for g in sig])
+    gd = np.array([np.asarray(g["g"]) / np.linalg.norm(g["g"]) for g in sig])
+    ctx.solve(q[:1], gd[:1], rtol=1e-12, max_iterations=20000)            # warm-up (set-up of the folded system)
+    timed = _event_timer(stream, flush)
+    ms, out = timed(lambda: ctx.solve(q, gd, rtol=1e-12, max_iterations=20000))
+    err = [abs(float(out["signal"][i]) - g["signal"]) / abs(g["signal"]) for i, g in enumerate(sig)]
+    info = ctx.strong_periodic_info()
+    st = out["stats"]
+    ctx.close()
+    return {"workload": "strong pseudo-periodic box: 12^3 Kuhn cubes of 4/3 um, z-cylinder r 5 um, periodic x/y/z, "
+                        "D 3e-3/2e-3, kappa 1e-5, PGSE 10600/43100 us, 270 steps",
+            "precision": "fp64", "solver": "Jacobi-BiCGSTAB, rtol 1e-12", "signals": len(sig),
+            "value": len(sig) / (ms / 1e3), "unit": "signals/s", "ms": ms,
+            "folded_dofs": info["n_dofs"], "vertex_classes": info["n_classes"],
+            "iterations_per_signal": st["total_iterations"] / len(sig),
+            "rel_err_vs_oracle": err, "max_rel_err_vs_oracle": max(err)}
+
+
 def cfg5_leg(args, pkg, stream, flush, peak, peak_src, traffic):
     """The uneven batch: 16 seeded boxes of 24^3 ... 96^3 Kuhn cubes of 0.5 um
     (edge counts stepped evenly) with random non-overlapping z-cylinders (radii
@@ -729,6 +775,8 @@ def main():
                     help="signals of the batched-adjoint leg on the 48^3 layered sphere (0: skip)")
     ap.add_argument("--uneven-meshes", type=int, default=16,
                     help="meshes of the uneven multi-mesh leg (0: skip)")
+    ap.add_argument("--strong-signals", type=int, default=4,
+                    help="signals of the strong pseudo-periodic leg (0: skip)")
     ap.add_argument("--cfg5", type=int, default=0,
                     help="signals per mesh of the 16-mesh 24^3..96^3 forward + adjoint leg (128: the whole "
                          "workload, several minutes; 0: skip)")

@@ -158,3 +158,27 @@ def test_reference_api(pkg, lib):
     dom.Apply()
     w = sim.solve(dom, para)
     assert abs(w - s) > 1e-6 * abs(s)
+
+
+def test_full_schedule_matches_golden(pkg, lib):
+    """270 steps on the 12^3 periodic box of tests/golden/oracle_strong_signals.json
+    (made by tests/golden/make_strong_fixture.py from the oracle)."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "oracle_strong_signals.json")) as fh:
+        gold = json.load(fh)
+    s = gold["setup"]
+    lo, hi = s["box"]
+    xyz, tets = pkg.meshgen.kuhn_box(lo, hi, s["cubes_per_axis"])
+    reg = cube_cylinder_regions(xyz, tets, s["radius"])
+    seq = pkg.sequences.pgse(s["delta"], s["Delta"])
+    kp = np.array([[0.0, s["kappa"]], [s["kappa"], 0.0]])
+    ctx = strong_ctx(pkg, xyz, tets, reg, 2, s["D"], None, kp, s["periodic_dir"], seq, s["dt"])
+    q = [g["q"] for g in gold["signals"]]
+    gd = [np.asarray(g["g"]) / np.linalg.norm(g["g"]) for g in gold["signals"]]
+    out = ctx.solve(q, gd, rtol=1e-13, max_iterations=20000, compartments=True)
+    assert ctx.strong_periodic_info()["n_dofs"] == gold["n_dofs"]
+    for i, g in enumerate(gold["signals"]):
+        assert abs(out["signal"][i] - g["signal"]) <= SIG_RTOL * abs(g["signal"]), (i, out["signal"][i], g["signal"])
+        assert np.allclose(out["compartments"][i], g["compartments"], rtol=1e-9)
+    ctx.close()
