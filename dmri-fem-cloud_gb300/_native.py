@@ -35,6 +35,7 @@ EXPORTS = [
     "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
     "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info", "bt_adjoint_batch", "bt_adjoint_multi",
     "bt_set_kappa_mode", "bt_set_schedule_integral", "bt_set_periodic_mode", "bt_strong_periodic_info",
+    "bt_adjoint_cells",
 ]
 
 
@@ -113,6 +114,8 @@ def load(path=None):
         "bt_signal_noalloc": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
         "bt_adjoint": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_double, C.c_int32, C.c_int32,
                                  _D, _D, _D, _D, C.POINTER(Stats)]),
+        "bt_adjoint_cells": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_double, C.c_int32, C.c_int32,
+                                       _D, _D, _D, _D, C.POINTER(Stats)]),
         "bt_tangent": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_int32, C.c_int32, C.c_int32, C.c_double,
                                  C.c_int32, _D, _D, C.POINTER(Stats)]),
         "bt_solve_multi": (C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _D, _I32, C.c_double, C.c_int32,
@@ -314,6 +317,23 @@ class Context:
                                         C.byref(st)))
         return {"signal": float(sig[0]), "dD": dD, "dinvT2": dT, "dkappa": dK.reshape(nr, nr),
                 "stats": st.as_dict()}
+
+    def adjoint_cells(self, q, gdir, sequence=0, u0=None, rtol=1e-13, max_iterations=5000, stride=0):
+        """Signal and its derivatives (unnormalised) w.r.t. a per-cell diffusion
+        tensor dD_cell[n_cells, 6] (xx, yy, zz, xy, xz, yz), a per-cell 1/T2
+        dinvT2_cell[n_cells] and the pair permeabilities, by the FP64 adjoint."""
+        g = np.ascontiguousarray(np.asarray(gdir, np.float64).reshape(3))
+        u = None if u0 is None else np.ascontiguousarray(np.asarray(u0, np.float64).reshape(self.n_vertices))
+        nr, nt = self.n_regions, self.info()["n_cells"]
+        sig = np.zeros(1)
+        d6, dT = np.zeros(nt * 6), np.zeros(nt)
+        dK = np.zeros(nr * nr)
+        st = Stats()
+        self._check(self.lib.bt_adjoint_cells(self.h, float(q), _dp(g), int(sequence), _dp(u), float(rtol),
+                                              int(max_iterations), int(stride), _dp(sig), _dp(d6), _dp(dT),
+                                              _dp(dK), C.byref(st)))
+        return {"signal": float(sig[0]), "dD_cell": d6.reshape(nt, 6), "dinvT2_cell": dT,
+                "dkappa": dK.reshape(nr, nr), "stats": st.as_dict()}
 
     def adjoint_batch(self, q, gdir, sequence=None, rtol=1e-9, max_iterations=20000, stride=0):
         """The discrete adjoint of many signals at once in mixed precision:

@@ -12,9 +12,15 @@ mixed-precision adjoint (``bt_adjoint_batch``: the signals advance together,
 forward and backward): it returns the n normalised signals, and its backward
 contracts the incoming gradient with the n per-signal derivatives.
 
+``BlochTorreyCellField.apply(D_cell[n_cells, 6], invT2_cell[n_cells], engine, q,
+gdir, sequence)`` is the field form: a per-cell diffusion tensor (xx, yy, zz,
+xy, xz, yz) and a per-cell 1/T2 go into the FP64 solve, and the backward
+returns dS/dD_cell and dS/d(1/T2)_cell from ``bt_adjoint_cells`` (for fitting
+a diffusivity or relaxation map).
+
 The tissue parameters may be CPU or CUDA tensors of any floating dtype; they
-are read on the host (they are a handful of numbers, not the field) and the
-gradients are returned on the parameters' own device and dtype.
+are read on the host and the gradients are returned on the parameters' own
+device and dtype.
 """
 
 import numpy as np
@@ -63,3 +69,23 @@ class BlochTorreySignals(torch.autograd.Function):
         outs = [torch.tensordot(g, t, dims=1) for t in (gD, gT, gK)]
         outs = [t.to(dev, dt) for t, (dev, dt) in zip(outs, ctx.like)]
         return outs[0], outs[1], outs[2], None, None, None, None
+
+
+class BlochTorreyCellField(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, D_cell, invT2_cell, engine, q, gdir, sequence=0):
+        engine.set_cell_diffusion(np.ascontiguousarray(_host(D_cell).reshape(-1, 6)))
+        engine.set_cell_T2(np.ascontiguousarray(_host(invT2_cell).reshape(-1)))
+        engine.assemble()
+        out = engine.adjoint_cells(q, gdir, sequence)
+        S0 = engine.info()["volume"]
+        ctx.like = [(x.device, x.dtype) for x in (D_cell, invT2_cell)]
+        ctx.save_for_backward(torch.from_numpy(out["dD_cell"] / S0), torch.from_numpy(out["dinvT2_cell"] / S0))
+        return torch.tensor(out["signal"] / S0, dtype=D_cell.dtype, device=D_cell.device)
+
+    @staticmethod
+    def backward(ctx, grad):
+        g = float(grad.detach().to("cpu", torch.float64))
+        gD, gT = ctx.saved_tensors                          # [n_cells, 6], [n_cells]
+        (dD, tD), (dT, tT) = ctx.like
+        return (g * gD).to(dD, tD), (g * gT).to(dT, tT), None, None, None, None

@@ -500,6 +500,30 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
     });
 }
 
+int bt_adjoint_cells(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0, double rtol,
+                     int32_t max_iterations, int32_t checkpoint_stride, double* signal_out, double* dS_dD_cell,
+                     double* dS_dinvT2_cell, double* dS_dkappa, bt_stats* stats) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint_cells: mesh not assembled");
+        BT_REQUIRE(!bt::strong_active(ctx), BT_ERR_STATE,
+                   "bt_adjoint_cells: not defined with the strong pseudo-periodic form");
+        BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_adjoint_cells: no schedule");
+        BT_REQUIRE(gdir && signal_out, BT_ERR_INVALID, "bt_adjoint_cells: bad arguments");
+        BT_REQUIRE(std::isfinite(q) && std::isfinite(gdir[0]) && std::isfinite(gdir[1]) && std::isfinite(gdir[2]),
+                   BT_ERR_INVALID, "bt_adjoint_cells: q and gdir must be finite");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_adjoint_cells: rtol must be > 0 and max_iterations >= 1");
+        if (u0)
+            for (int64_t v = 0; v < ctx->mesh.n_v; ++v)
+                BT_REQUIRE(std::isfinite(u0[v]), BT_ERR_INVALID, "bt_adjoint_cells: u0 must be finite");
+        use_device(ctx);
+        bt::adjoint_fp64(ctx, q, gdir, sequence, u0, rtol, max_iterations, checkpoint_stride, signal_out, nullptr,
+                         nullptr, dS_dkappa, stats, dS_dD_cell, dS_dinvT2_cell);
+        ctx->last_precision = -1;
+    });
+}
+
 int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir, const int32_t* sequence,
                      double rtol, int32_t max_iterations, int32_t checkpoint_stride, double* signal_out,
                      double* dS_dD, double* dS_dinvT2, double* dS_dkappa, bt_stats* stats) {

@@ -232,7 +232,8 @@ void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir,
 void get_solution_fp64(bt_ctx* ctx, int32_t index, double* u);
 void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const double* u0, double rtol,
                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
-                  bt_stats* st);
+                  bt_stats* st,
+                  double* dD_cell = nullptr, double* dinvT2_cell = nullptr);
 void get_solution_mixed(bt_ctx* ctx, int32_t index, double* u);
 void tangent_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const double* u0, int32_t kind, int32_t ri,
                   int32_t rj, double rtol, int32_t maxit, double* sig, double* dsig, bt_stats* st);

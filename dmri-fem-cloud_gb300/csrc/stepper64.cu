@@ -702,11 +702,14 @@ namespace bt {
 // (default ceil(sqrt(N))).
 namespace {
 
+// acc6 (nullable): per cell, the contraction with the unit stiffness of each
+// stored tensor component (xx, yy, zz, xy, xz, yz; an off-diagonal component
+// sets both D_kl and D_lk), for gradients with respect to a per-cell D field.
 __global__ void k_adj_cells(int64_t n_t, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
                             const int32_t* __restrict__ comp, const int32_t* __restrict__ dof_of, int nc,
                             const double2* __restrict__ lam, const double2* __restrict__ un,
                             const double2* __restrict__ un1, double theta, double* __restrict__ accD,
-                            double* __restrict__ accT) {
+                            double* __restrict__ accT, double* __restrict__ acc6) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_t) return;
     const int4 qv = reinterpret_cast<const int4*>(tets)[t];
@@ -758,6 +761,29 @@ __global__ void k_adj_cells(int64_t n_t, const double* __restrict__ xyz, const i
         }
     accD[t] -= sK;
     accT[t] -= sM;
+    if (acc6) {
+        // Re(L^T (grad phi_r)_k (grad phi_c)_l V) summed over r, c = (L^T G)_k . (G^T V)_l
+        double lg[3][2], gv[3][2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lg[k][0] = lg[k][1] = gv[k][0] = gv[k][1] = 0.0;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                lg[k][0] += G[r][k] * L[r].x;
+                lg[k][1] += G[r][k] * L[r].y;
+                gv[k][0] += G[r][k] * V[r].x;
+                gv[k][1] += G[r][k] * V[r].y;
+            }
+        }
+        auto re = [&](int k, int l) { return lg[k][0] * gv[l][0] - lg[k][1] * gv[l][1]; };
+        double* o = acc6 + t * 6;
+        o[0] -= vol * re(0, 0);
+        o[1] -= vol * re(1, 1);
+        o[2] -= vol * re(2, 2);
+        o[3] -= vol * (re(0, 1) + re(1, 0));
+        o[4] -= vol * (re(0, 2) + re(2, 0));
+        o[5] -= vol * (re(1, 2) + re(2, 1));
+    }
 }
 
 __global__ void k_adj_facets(int64_t n_if, const int32_t* __restrict__ fcell, const int32_t* __restrict__ fface,
@@ -814,14 +840,16 @@ __global__ void k_adj_facets(int64_t n_if, const int32_t* __restrict__ fcell, co
 
 void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const double* u0, double rtol,
                   int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
-                  bt_stats* st) {
+                  bt_stats* st, double* dD_cell, double* dinvT2_cell) {
     Mesh& m = ctx->mesh;
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
-    BT_REQUIRE(!ctx->coeffs.has_cell_D, BT_ERR_STATE,
-               "bt_adjoint: gradients are defined for per-region isotropic D (clear the per-cell tensor)");
-    BT_REQUIRE(!ctx->coeffs.has_cell_T2, BT_ERR_STATE,
-               "bt_adjoint: gradients are defined for per-region 1/T2 (clear the per-cell T2)");
+    BT_REQUIRE(!(dD && ctx->coeffs.has_cell_D), BT_ERR_STATE,
+               "bt_adjoint: per-region D gradients need per-region isotropic D (clear the per-cell tensor, or "
+               "use bt_adjoint_cells)");
+    BT_REQUIRE(!(dinvT2 && ctx->coeffs.has_cell_T2), BT_ERR_STATE,
+               "bt_adjoint: per-region 1/T2 gradients need per-region 1/T2 (clear the per-cell T2, or use "
+               "bt_adjoint_cells)");
     BT_REQUIRE(!ctx->per.on, BT_ERR_STATE,
                "bt_adjoint: not defined with pseudo-periodic boundaries (the mirror term is not transposed)");
     BT_REQUIRE(!ctx->coeffs.kappa_cr, BT_ERR_STATE,
@@ -860,6 +888,11 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
     accD.zero(s);
     accT.alloc(m.n_t);
     accT.zero(s);
+    DevBuf<double> acc6;
+    if (dD_cell) {
+        acc6.alloc((size_t)m.n_t * 6);
+        acc6.zero(s);
+    }
     accK.alloc(std::max<int64_t>(1, m.n_iface));
     accK.zero(s);
     std::vector<int32_t> hit;
@@ -900,7 +933,7 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
             const double2* un = seg.p + (size_t)(n - a0) * W.n_pad;
             const double2* un1 = seg.p + (size_t)(n - a0 + 1) * W.n_pad;
             k_adj_cells<<<cb, 128, 0, s>>>(m.n_t, m.xyz, m.tets, m.comp, m.dof_of, m.n_comp, lam.p, un, un1, th,
-                                           accD.p, accT.p);
+                                           accD.p, accT.p, dD_cell ? acc6.p : nullptr);
             if (m.n_iface > 0)
                 k_adj_facets<<<fb, 128, 0, s>>>(m.n_iface, m.iface_cell, m.iface_face, m.xyz, m.tets, m.nbr,
                                                 m.comp, m.dof_of, m.n_comp, lam.p, un, un1, th, accK.p);
@@ -928,6 +961,8 @@ void adjoint_fp64(bt_ctx* ctx, double q, const double* gdir, int32_t seq, const 
     }
     m.region.download(hreg.data(), m.n_t, s);
     m.nbr.download(hnb.data(), m.n_t * 4, s);
+    if (dD_cell) acc6.download(dD_cell, (size_t)m.n_t * 6, s);
+    if (dinvT2_cell) accT.download(dinvT2_cell, m.n_t, s);
     BT_CUDA(cudaEventRecord(ctx->ev2, s));
     BT_CUDA(cudaStreamSynchronize(s));
     const int nr = m.n_regions;

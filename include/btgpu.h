@@ -273,6 +273,18 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
                double* signal_out, double* dS_dD, double* dS_dinvT2, double* dS_dkappa,
                bt_stats* stats);
 
+/* The same adjoint with per-cell fields: dS_dD_cell[n_cells*6] is the derivative
+ * with respect to the stored components (xx, yy, zz, xy, xz, yz) of a per-cell
+ * diffusion tensor (an off-diagonal component sets D_kl and D_lk together, as in
+ * bt_set_cell_diffusion) and dS_dinvT2_cell[n_cells] with respect to a per-cell
+ * 1/T2, both at the context's current coefficients (per-region or per-cell);
+ * dS_dkappa as in bt_adjoint.  The derivative with respect to an isotropic D of
+ * cell t is xx + yy + zz.  Any output pointer may be NULL. */
+int bt_adjoint_cells(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0,
+                     double rtol, int32_t max_iterations, int32_t checkpoint_stride,
+                     double* signal_out, double* dS_dD_cell, double* dS_dinvT2_cell, double* dS_dkappa,
+                     bt_stats* stats);
+
 /* The same discrete adjoint for n_signals signals at once in the batched mixed
  * precision stepper (FP32 Krylov vectors, double-float residuals; the backward
  * sweep is a forward sweep of the same kernel with the schedule pair

@@ -228,3 +228,79 @@ def test_multi_mesh_adjoint_matches_fp64(pkg, lib):
                 assert err <= 1e-5 * scale, (k, i, key, err / scale)
     for c in ctxs:
         c.close()
+
+
+def test_cell_field_gradients(pkg, lib):
+    """bt_adjoint_cells: the per-cell derivatives sum to the per-region ones
+    (isotropic D: xx + yy + zz of the region's cells; 1/T2), and with a per-cell
+    anisotropic tensor and per-cell T2 they match central differences of the
+    GPU forward (one component or 1/T2 moved on all cells of a region); the
+    autograd form returns them."""
+    xyz, tets, reg, D, invT2, kp = layered_case(pkg, n=6)
+    ctx, q = make(pkg, xyz, tets, reg, D, invT2, kp)
+    adj = ctx.adjoint(q, G, rtol=1e-14, max_iterations=20000)
+    cel = ctx.adjoint_cells(q, G, rtol=1e-14, max_iterations=20000)
+    assert abs(cel["signal"] - adj["signal"]) <= 1e-12 * abs(adj["signal"])
+    iso = cel["dD_cell"][:, :3].sum(axis=1)
+    for r in range(4):
+        m = reg == r
+        assert abs(iso[m].sum() - adj["dD"][r]) <= 1e-10 * np.max(np.abs(adj["dD"]))
+        assert abs(cel["dinvT2_cell"][m].sum() - adj["dinvT2"][r]) <= 1e-10 * np.max(np.abs(adj["dinvT2"]))
+    assert np.allclose(cel["dkappa"], adj["dkappa"], rtol=1e-12, atol=1e-12 * np.max(np.abs(adj["dkappa"])))
+    # anisotropic per-cell field
+    rng = np.random.default_rng(3)
+    n_t = len(tets)
+    D6 = np.zeros((n_t, 6))
+    D6[:, :3] = D[reg][:, None] * (1.0 + 0.3 * rng.random((n_t, 3)))
+    D6[:, 3:] = D[reg][:, None] * 0.1 * (rng.random((n_t, 3)) - 0.5)
+    iT = invT2[reg] + 1e-5 * rng.random(n_t)
+    ctx.set_cell_diffusion(D6)
+    ctx.set_cell_T2(iT)
+    ctx.assemble()
+    cel = ctx.adjoint_cells(q, G, rtol=1e-14, max_iterations=20000)
+
+    def sig6(D6x, iTx):
+        ctx.set_cell_diffusion(D6x)
+        ctx.set_cell_T2(iTx)
+        ctx.assemble()
+        return ctx.solve([q], G, rtol=1e-14, max_iterations=20000)["signal"][0]
+
+    # central differences of a component over the cells of one region (a single
+    # cell's derivative is below the differences' rounding)
+    base = sig6(D6, iT)
+    assert abs(base - cel["signal"]) <= 1e-10 * abs(base)
+    for r, k in ((1, 0), (1, 3), (2, 5), (0, 4)):
+        m = reg == r
+        h = 1e-6 * 3e-3
+        Dp, Dm = D6.copy(), D6.copy()
+        Dp[m, k] += h
+        Dm[m, k] -= h
+        fd = (sig6(Dp, iT) - sig6(Dm, iT)) / (2 * h)
+        ad = cel["dD_cell"][m, k].sum()
+        scale = np.max(np.abs([cel["dD_cell"][reg == rr, kk].sum() for rr in range(4) for kk in range(6)]))
+        assert abs(ad - fd) <= ADJ_RTOL * scale, (r, k, ad, fd)
+    for r in (1, 2):
+        m = reg == r
+        h = 1e-6 * 1e-5
+        Tp, Tm = iT.copy(), iT.copy()
+        Tp[m] += h
+        Tm[m] -= h
+        fd = (sig6(D6, Tp) - sig6(D6, Tm)) / (2 * h)
+        ad = cel["dinvT2_cell"][m].sum()
+        scale = np.max(np.abs([cel["dinvT2_cell"][reg == rr].sum() for rr in range(4)]))
+        assert abs(ad - fd) <= ADJ_RTOL * scale, (r, ad, fd)
+    # autograd over the fields
+    import importlib
+    import torch
+    ag = importlib.import_module(pkg.__name__ + ".autograd")
+    Dt = torch.tensor(D6, requires_grad=True)
+    Tt = torch.tensor(iT, requires_grad=True)
+    s = ag.BlochTorreyCellField.apply(Dt, Tt, ctx, q, G, 0)
+    s.backward()
+    S0 = ctx.info()["volume"]
+    # (the autograd form runs the adjoint at its default rtol 1e-13, the reference above at 1e-14)
+    gs = np.max(np.abs(cel["dD_cell"])) / S0
+    assert np.max(np.abs(Dt.grad.numpy() - cel["dD_cell"] / S0)) <= 1e-8 * gs
+    gt = np.max(np.abs(cel["dinvT2_cell"])) / S0
+    assert np.max(np.abs(Tt.grad.numpy() - cel["dinvT2_cell"] / S0)) <= 1e-8 * gt
+    ctx.close()
