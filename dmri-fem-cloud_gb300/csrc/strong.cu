@@ -760,7 +760,10 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
     int per_sm = 0;
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_sbc, kThreadsS, 0));
     BT_REQUIRE(per_sm >= 1, BT_ERR_CUDA, "strong periodic stepper does not fit on an SM");
-    const int64_t need = (n + kThreadsS - 1) / kThreadsS;
+    // one thread per row at least, and (small systems) one block per SM with >= 16
+    // rows each: the stepper is bound by FP64 latency, so it spreads over the SMs
+    const int64_t need = std::max<int64_t>((n + kThreadsS - 1) / kThreadsS,
+                                           std::min<int64_t>(ctx->num_sms, (n + 15) / 16));
     P.nblocks = (int32_t)std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * ctx->num_sms, need));
     P.are.alloc(nnz);
     P.mdg.alloc(nnz);
