@@ -519,9 +519,9 @@ def batched_leg(args, pkg, stream, flush, peak, peak_src, traffic):
 
 def adjoint_leg(args, pkg, stream, flush, peak, peak_src, traffic):
     """Gradients: the layered-sphere 48^3 workload (4 layers, per-layer D and T2,
-    per-interface kappa), `adjoint_signals` of its 120 signals spread evenly;
-    the batched mixed-precision adjoint (bt_adjoint_batch, one set of launches)
-    against the FP64 adjoint (bt_adjoint) of three of them."""
+    per-interface kappa), `adjoint_signals` of its 120 signals spread evenly
+    (default: all 120); the batched mixed-precision adjoint (bt_adjoint_batch)
+    against the FP64 adjoint (bt_adjoint) of five spread signals."""
     w = pkg.meshgen.workload("cfg4")
     sig = w["signals"]
     idx = np.linspace(0, len(sig) - 1, args.adjoint_signals).astype(int)
@@ -531,7 +531,7 @@ def adjoint_leg(args, pkg, stream, flush, peak, peak_src, traffic):
     timed = _event_timer(stream, flush)
     ctx.solve(q, g, None, None, pkg.PRECISION_MIXED, 1e-9, args.maxit)          # warm-up (autotuner)
     ms_b, out = timed(lambda: ctx.adjoint_batch(q, g, rtol=1e-9, max_iterations=args.maxit))
-    chk = sorted({0, len(q) // 2, len(q) - 1})
+    chk = sorted(set(np.linspace(0, len(q) - 1, min(5, len(q))).astype(int).tolist()))
     ms_64 = []
     err = {"dD": 0.0, "dinvT2": 0.0, "dkappa": 0.0}
     sig_err = 0.0
@@ -771,7 +771,7 @@ def main():
     ap.add_argument("--batched-signals", type=int, default=512,
                     help="signals of the eight-cylinder 64^3 batched leg (0: skip)")
     ap.add_argument("--fp64-sample", type=int, default=8, help="FP64 signals timed against the batched leg")
-    ap.add_argument("--adjoint-signals", type=int, default=16,
+    ap.add_argument("--adjoint-signals", type=int, default=120,
                     help="signals of the batched-adjoint leg on the 48^3 layered sphere (0: skip)")
     ap.add_argument("--uneven-meshes", type=int, default=16,
                     help="meshes of the uneven multi-mesh leg (0: skip)")

@@ -35,7 +35,7 @@ EXPORTS = [
     "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
     "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info", "bt_adjoint_batch", "bt_adjoint_multi",
     "bt_set_kappa_mode", "bt_set_schedule_integral", "bt_set_periodic_mode", "bt_strong_periodic_info",
-    "bt_adjoint_cells",
+    "bt_adjoint_cells", "bt_adjoint_batch_cells",
 ]
 
 
@@ -116,6 +116,8 @@ def load(path=None):
                                  _D, _D, _D, _D, C.POINTER(Stats)]),
         "bt_adjoint_cells": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_double, C.c_int32, C.c_int32,
                                        _D, _D, _D, _D, C.POINTER(Stats)]),
+        "bt_adjoint_batch_cells": (C.c_int, [_P, C.c_int32, _D, _D, _I32, _D, C.c_double, C.c_int32, C.c_int32,
+                                             _D, _D, _D, _D, C.POINTER(Stats)]),
         "bt_tangent": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_int32, C.c_int32, C.c_int32, C.c_double,
                                  C.c_int32, _D, _D, C.POINTER(Stats)]),
         "bt_solve_multi": (C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _D, _I32, C.c_double, C.c_int32,
@@ -334,6 +336,25 @@ class Context:
                                               _dp(dK), C.byref(st)))
         return {"signal": float(sig[0]), "dD_cell": d6.reshape(nt, 6), "dinvT2_cell": dT,
                 "dkappa": dK.reshape(nr, nr), "stats": st.as_dict()}
+
+    def adjoint_batch_cells(self, q, gdir, weights, sequence=None, rtol=1e-9, max_iterations=20000, stride=0):
+        """Per-cell gradients of sum_s weights[s] S_s (unnormalised) by the batched
+        mixed-precision adjoint: signal[n], dD_cell[n_cells, 6], dinvT2_cell[n_cells],
+        dkappa[nr, nr]."""
+        q = np.ascontiguousarray(np.atleast_1d(np.asarray(q, np.float64)))
+        n = len(q)
+        g = np.ascontiguousarray(np.asarray(gdir, np.float64).reshape(n, 3))
+        w = np.ascontiguousarray(np.asarray(weights, np.float64).reshape(n))
+        seq = None if sequence is None else np.ascontiguousarray(np.asarray(sequence, np.int32).reshape(n))
+        nr, nt = self.n_regions, self.info()["n_cells"]
+        sig = np.zeros(n)
+        d6, dT, dK = np.zeros(nt * 6), np.zeros(nt), np.zeros(nr * nr)
+        st = Stats()
+        self._check(self.lib.bt_adjoint_batch_cells(self.h, n, _dp(q), _dp(g), _ip(seq), _dp(w), float(rtol),
+                                                    int(max_iterations), int(stride), _dp(sig), _dp(d6), _dp(dT),
+                                                    _dp(dK), C.byref(st)))
+        return {"signal": sig, "dD_cell": d6.reshape(nt, 6), "dinvT2_cell": dT, "dkappa": dK.reshape(nr, nr),
+                "stats": st.as_dict()}
 
     def adjoint_batch(self, q, gdir, sequence=None, rtol=1e-9, max_iterations=20000, stride=0):
         """The discrete adjoint of many signals at once in mixed precision:

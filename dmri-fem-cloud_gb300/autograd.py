@@ -18,6 +18,12 @@ xy, xz, yz) and a per-cell 1/T2 go into the FP64 solve, and the backward
 returns dS/dD_cell and dS/d(1/T2)_cell from ``bt_adjoint_cells`` (for fitting
 a diffusivity or relaxation map).
 
+``BlochTorreyCellFields.apply(D_cell, invT2_cell, engine, q[n], gdir[n, 3],
+sequence[n] or None)`` returns n normalised signals of the mixed-precision
+batched solve with those fields; its backward runs the batched adjoint once with
+the incoming gradient as signal weights (``bt_adjoint_batch_cells``) and returns
+the per-cell gradients.
+
 The tissue parameters may be CPU or CUDA tensors of any floating dtype; they
 are read on the host and the gradients are returned on the parameters' own
 device and dtype.
@@ -89,3 +95,26 @@ class BlochTorreyCellField(torch.autograd.Function):
         gD, gT = ctx.saved_tensors                          # [n_cells, 6], [n_cells]
         (dD, tD), (dT, tT) = ctx.like
         return (g * gD).to(dD, tD), (g * gT).to(dT, tT), None, None, None, None
+
+
+class BlochTorreyCellFields(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, D_cell, invT2_cell, engine, q, gdir, sequence=None):
+        engine.set_cell_diffusion(np.ascontiguousarray(_host(D_cell).reshape(-1, 6)))
+        engine.set_cell_T2(np.ascontiguousarray(_host(invT2_cell).reshape(-1)))
+        engine.assemble()
+        q = np.atleast_1d(np.asarray(q, np.float64))
+        gdir = np.asarray(gdir, np.float64).reshape(len(q), 3)
+        out = engine.solve(q, gdir, sequence, None, 1, 1e-9, 20000)     # mixed precision
+        S0 = engine.info()["volume"]
+        ctx.engine, ctx.q, ctx.gdir, ctx.sequence, ctx.S0 = engine, q, gdir, sequence, S0
+        ctx.like = [(x.device, x.dtype) for x in (D_cell, invT2_cell)]
+        return torch.from_numpy(out["signal"] / S0).to(D_cell.device, D_cell.dtype)
+
+    @staticmethod
+    def backward(ctx, grad):
+        w = grad.detach().to("cpu", torch.float64).numpy() / ctx.S0
+        out = ctx.engine.adjoint_batch_cells(ctx.q, ctx.gdir, w, ctx.sequence)
+        (dD, tD), (dT, tT) = ctx.like
+        return (torch.from_numpy(out["dD_cell"]).to(dD, tD), torch.from_numpy(out["dinvT2_cell"]).to(dT, tT),
+                None, None, None, None)

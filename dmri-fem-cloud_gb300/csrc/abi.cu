@@ -547,6 +547,31 @@ int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const doub
     });
 }
 
+int bt_adjoint_batch_cells(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir,
+                           const int32_t* sequence, const double* weights, double rtol, int32_t max_iterations,
+                           int32_t checkpoint_stride, double* signal_out, double* dS_dD_cell, double* dS_dinvT2_cell,
+                           double* dS_dkappa, bt_stats* stats) {
+    if (!ctx) return BT_ERR_INVALID;
+    return guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint_batch_cells: mesh not assembled");
+        BT_REQUIRE(!bt::strong_active(ctx), BT_ERR_STATE,
+                   "bt_adjoint_batch_cells: not defined with the strong pseudo-periodic form");
+        BT_REQUIRE(ctx->sched.set, BT_ERR_STATE, "bt_adjoint_batch_cells: no schedule");
+        BT_REQUIRE(n_signals >= 1 && q && gdir && weights && signal_out, BT_ERR_INVALID,
+                   "bt_adjoint_batch_cells: bad arguments");
+        BT_REQUIRE(std::isfinite(rtol) && rtol > 0.0 && max_iterations >= 1, BT_ERR_INVALID,
+                   "bt_adjoint_batch_cells: rtol must be > 0 and max_iterations >= 1");
+        for (int32_t i = 0; i < n_signals; ++i)
+            BT_REQUIRE(std::isfinite(q[i]) && std::isfinite(gdir[3 * i]) && std::isfinite(gdir[3 * i + 1]) &&
+                           std::isfinite(gdir[3 * i + 2]) && std::isfinite(weights[i]),
+                       BT_ERR_INVALID, "bt_adjoint_batch_cells: q, gdir and weights must be finite");
+        use_device(ctx);
+        ctx->last_precision = -1;
+        bt::adjoint_mixed(ctx, n_signals, q, gdir, sequence, rtol, max_iterations, checkpoint_stride, signal_out,
+                          nullptr, nullptr, dS_dkappa, stats, weights, dS_dD_cell, dS_dinvT2_cell);
+    });
+}
+
 int bt_adjoint_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_signals, const double* q,
                      const double* gdir, const int32_t* sequence, double rtol, int32_t max_iterations,
                      int32_t checkpoint_stride, double* signal_out, double* dS_dD, double* dS_dinvT2,

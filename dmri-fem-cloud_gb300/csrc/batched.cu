@@ -2377,6 +2377,79 @@ __global__ void k_adjb_cells(int64_t n_t, int NS, int ns, const float4* __restri
     accT[idx] -= (double)sM;
 }
 
+// Per-cell gradients of a weighted sum of the batch's signals, sum_s w_s S_s: one
+// warp per cell, lanes over signals, the contraction of k_adjb_cells split into
+// the six stored tensor components (xx, yy, zz, xy, xz, yz; an off-diagonal one
+// counts D_kl and D_lk) and the mass term; the lanes' sums are added in a fixed
+// order (warp tree), so the result is deterministic.
+__global__ void k_adjb_cells_w(int64_t n_t, int NS, int ns, const float4* __restrict__ geo,
+                               const int32_t* __restrict__ tets, const int32_t* __restrict__ comp,
+                               const int32_t* __restrict__ dof_of, int nc, const float2* __restrict__ lh,
+                               const float2* __restrict__ ll, const float2* __restrict__ u0h,
+                               const float2* __restrict__ u0l, const float2* __restrict__ u1h,
+                               const float2* __restrict__ u1l, double theta, const double* __restrict__ wsig,
+                               double* __restrict__ acc6, double* __restrict__ accT) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float th = (float)theta, om = (float)(1.0 - theta);
+    for (int64_t t = warp; t < n_t; t += nwarps) {
+        const int f = comp[t];
+        size_t base[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) base[k] = (size_t)dof_of[(int64_t)tets[t * 4 + k] * nc + f] * ns;
+        const float4 a = geo[t * 3 + 0], b = geo[t * 3 + 1], c = geo[t * 3 + 2];
+        const float G[3][3] = {{a.x, a.y, a.z}, {a.w, b.x, b.y}, {b.z, b.w, c.x}};
+        const double vol = (double)c.y;
+        double o[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int sg = lane; sg < NS; sg += 32) {
+            float2 gl[3], gv[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) gl[d] = gv[d] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 1; k < 4; ++k) {
+                const float2 dl = df_diff(lh, ll, base[k] + sg, base[0] + sg);
+                const float2 d0 = df_diff(u0h, u0l, base[k] + sg, base[0] + sg),
+                             d1 = df_diff(u1h, u1l, base[k] + sg, base[0] + sg);
+                const float2 dv = make_float2(th * d1.x + om * d0.x, th * d1.y + om * d0.y);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    gl[d].x = fmaf(dl.x, G[k - 1][d], gl[d].x);
+                    gl[d].y = fmaf(dl.y, G[k - 1][d], gl[d].y);
+                    gv[d].x = fmaf(dv.x, G[k - 1][d], gv[d].x);
+                    gv[d].y = fmaf(dv.y, G[k - 1][d], gv[d].y);
+                }
+            }
+            auto re = [&](int k, int l) { return gl[k].x * gv[l].x - gl[k].y * gv[l].y; };
+            float2 sl = make_float2(0.f, 0.f), sv = sl;
+            float sd = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float2 L = lh[base[k] + sg], A0 = u0h[base[k] + sg], A1 = u1h[base[k] + sg];
+                const float2 V = make_float2(th * A1.x + om * A0.x, th * A1.y + om * A0.y);
+                sl.x += L.x; sl.y += L.y;
+                sv.x += V.x; sv.y += V.y;
+                sd += L.x * V.x - L.y * V.y;
+            }
+            const double w = wsig[sg];
+            o[0] += w * (double)re(0, 0);
+            o[1] += w * (double)re(1, 1);
+            o[2] += w * (double)re(2, 2);
+            o[3] += w * (double)(re(0, 1) + re(1, 0));
+            o[4] += w * (double)(re(0, 2) + re(2, 0));
+            o[5] += w * (double)(re(1, 2) + re(2, 1));
+            o[6] += w * (double)(sl.x * sv.x - sl.y * sv.y + sd);
+        }
+#pragma unroll
+        for (int k = 0; k < 7; ++k) o[k] = warp_sum(o[k]);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) acc6[t * 6 + k] -= vol * o[k];
+            accT[t] -= vol / 20.0 * o[6];
+        }
+    }
+}
+
 __device__ __forceinline__ double2 state_at(const float2* __restrict__ h, const float2* __restrict__ l, size_t i) {
     const float2 a = h[i], b = l[i];
     return make_double2((double)a.x + (double)b.x, (double)a.y + (double)b.y);
@@ -2467,14 +2540,20 @@ struct AdjMesh {
     DevBuf<float4> cgeo;
     DevBuf<int32_t> pair;
     DevBuf<float2> ckh, ckl, sgh, sgl, bkh, bkl, lch, lcl;
+    // per-cell gradients of a weighted signal sum (nullable): weights of the
+    // batch's signals, accumulators over all batches
+    DevBuf<double> wsig;
+    double* acc6 = nullptr;
+    double* accTc = nullptr;
 };
 
-static void adj_mesh_setup(AdjMesh& A, bt_ctx* ctx) {
+static void adj_mesh_setup(AdjMesh& A, bt_ctx* ctx, bool cells = false) {
     Mesh& m = ctx->mesh;
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
-    BT_REQUIRE(!ctx->coeffs.has_cell_D && !ctx->coeffs.has_cell_T2, BT_ERR_STATE,
-               "batched adjoint: gradients are defined for per-region coefficients (clear per-cell D / T2)");
+    BT_REQUIRE(cells || (!ctx->coeffs.has_cell_D && !ctx->coeffs.has_cell_T2), BT_ERR_STATE,
+               "batched adjoint: per-region gradients need per-region coefficients (clear per-cell D / T2, or use "
+               "bt_adjoint_batch_cells)");
     BT_REQUIRE(!ctx->per.on, BT_ERR_STATE, "batched adjoint: not defined with pseudo-periodic boundaries");
     BT_REQUIRE(!ctx->coeffs.kappa_cr, BT_ERR_STATE,
                "batched adjoint: gradients are defined for one permeability per facet (not the Crouzeix-Raviart mode)");
@@ -2550,6 +2629,12 @@ static void adj_contract(AdjMesh& A, int n, int a0, int e0, double theta) {
         k_adjb_facets<<<fb, 256, 0, s>>>(m.n_iface, A.NS, A.ns, m.iface_cell, m.iface_face, m.xyz, m.tets, m.nbr,
                                          m.comp, m.dof_of, m.n_comp, Lh, Ll, A.sgh.p + o0, A.sgl.p + o0,
                                          A.sgh.p + o1, A.sgl.p + o1, theta, A.accK);
+    if (A.acc6) {
+        const unsigned wb = (unsigned)std::min<int64_t>((m.n_t + 7) / 8, (int64_t)A.ctx->num_sms * 64);
+        k_adjb_cells_w<<<wb, 256, 0, s>>>(m.n_t, A.NS, A.ns, A.cgeo, m.tets, m.comp, m.dof_of, m.n_comp, Lh, Ll,
+                                          A.sgh.p + o0, A.sgl.p + o0, A.sgh.p + o1, A.sgl.p + o1, theta, A.wsig,
+                                          A.acc6, A.accTc);
+    }
     BT_CUDA(cudaGetLastError());
 }
 
@@ -2683,11 +2768,21 @@ static int adj_stride(int N, int stride) {
 
 void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
                    int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
-                   bt_stats* st) {
+                   bt_stats* st, const double* weights, double* dD_cell, double* dinvT2_cell) {
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
     AdjMesh A;
-    adj_mesh_setup(A, ctx);
+    const bool cells = weights != nullptr;
+    adj_mesh_setup(A, ctx, cells);
+    DevBuf<double> acc6, accTc;
+    if (cells) {
+        acc6.alloc((size_t)ctx->mesh.n_t * 6);
+        acc6.zero(s);
+        accTc.alloc((size_t)ctx->mesh.n_t);
+        accTc.zero(s);
+        A.acc6 = acc6.p;
+        A.accTc = accTc.p;
+    }
     SolverMixed& W = *A.W;
     const int N = S.n_steps;
     stride = adj_stride(N, stride);
@@ -2711,10 +2806,13 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
                                8.0 * (2.0 * (double)m.n_t + (double)std::max<int64_t>(1, m.n_iface));
         cap = (int)std::max(1.0, std::min((double)cap, 0.25 * (double)free_b / per_sig));
     }
+    std::vector<double> kap_sig;
+    if (cells && dkappa) kap_sig.assign((size_t)nsig * ctx->mesh.n_regions * ctx->mesh.n_regions, 0.0);
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
     for (int32_t b0 = 0; b0 < nsig; b0 += cap) {
         const int NS = std::min<int32_t>(cap, nsig - b0);
         const int R = 2 * NS;
+        if (cells) A.wsig.upload(weights + b0, NS, s);
         upload_rhs(ctx, W, NS, q + b0, gdir + 3 * b0, seq ? seq + b0 : nullptr);
         const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, A.d_u0);
         adj_batch_alloc(A, NS, padded_rhs(R, geo.lpr), nck, stride);
@@ -2723,7 +2821,21 @@ void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdi
             return launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, n_steps, rtol, maxit, A.d_u0, &ex[0]);
         };
         adj_pipeline(G, N, stride, S.theta, launch, {(int)b0}, {sig}, ms, launches);
-        adj_finish(A, b0, dD, dinvT2, dkappa);
+        if (cells)
+            adj_finish(A, b0, nullptr, nullptr, dkappa ? kap_sig.data() : nullptr);
+        else
+            adj_finish(A, b0, dD, dinvT2, dkappa);
+    }
+    if (cells) {
+        const int nr2 = ctx->mesh.n_regions * ctx->mesh.n_regions;
+        if (dkappa)
+            for (int k = 0; k < nr2; ++k) {
+                double a = 0.0;
+                for (int32_t i = 0; i < nsig; ++i) a += weights[i] * kap_sig[(size_t)i * nr2 + k];
+                dkappa[k] = a;
+            }
+        if (dD_cell) acc6.download(dD_cell, (size_t)ctx->mesh.n_t * 6, s);
+        if (dinvT2_cell) accTc.download(dinvT2_cell, (size_t)ctx->mesh.n_t, s);
     }
     BT_CUDA(cudaEventRecord(ctx->ev2, s));
     BT_CUDA(cudaEventSynchronize(ctx->ev2));

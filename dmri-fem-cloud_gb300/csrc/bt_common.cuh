@@ -252,7 +252,8 @@ void free_strong(bt_ctx* ctx);
 void strong_directions(const bt_ctx* ctx, int32_t* dir);
 void adjoint_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq, double rtol,
                    int32_t maxit, int32_t stride, double* sig, double* dD, double* dinvT2, double* dkappa,
-                   bt_stats* st);
+                   bt_stats* st,
+                   const double* weights = nullptr, double* dD_cell = nullptr, double* dinvT2_cell = nullptr);
 void adjoint_mixed_multi(bt_ctx* const* ctxs, int32_t nm, const int32_t* nsig, const double* q, const double* gdir,
                          const int32_t* seq, double rtol, int32_t maxit, int32_t stride, double* sig, double* dD,
                          double* dinvT2, double* dkappa, bt_stats* st);

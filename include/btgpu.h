@@ -298,6 +298,20 @@ int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const doub
                      const int32_t* sequence, double rtol, int32_t max_iterations, int32_t checkpoint_stride,
                      double* signal_out, double* dS_dD, double* dS_dinvT2, double* dS_dkappa, bt_stats* stats);
 
+/* Per-cell gradients of a weighted sum of signals, sum_s weights[s] * S_s, by the
+ * batched mixed-precision adjoint (bt_adjoint_batch's pipeline): dS_dD_cell[n_cells*6]
+ * with respect to the stored components (xx, yy, zz, xy, xz, yz) of a per-cell
+ * diffusion tensor, dS_dinvT2_cell[n_cells] with respect to a per-cell 1/T2 (both at
+ * the context's current coefficients, per-region or per-cell) and
+ * dS_dkappa[n_regions*n_regions] with respect to the pair permeabilities; the
+ * signals themselves go to signal_out[n_signals].  This is the vector-Jacobian
+ * product autograd needs for a field: weights = the incoming gradient.  Output
+ * pointers other than signal_out may be NULL. */
+int bt_adjoint_batch_cells(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir,
+                           const int32_t* sequence, const double* weights, double rtol, int32_t max_iterations,
+                           int32_t checkpoint_stride, double* signal_out, double* dS_dD_cell, double* dS_dinvT2_cell,
+                           double* dS_dkappa, bt_stats* stats);
+
 /* bt_adjoint_batch for several meshes in one call: mesh m is the mesh,
  * coefficients, assembly and schedule of contexts[m] (all with the same number
  * of steps and theta) and gets n_signals[m] (1..256) signals; q, gdir, sequence
