@@ -67,7 +67,7 @@ struct Strong {
     int32_t nblocks = 0;
     DevBuf<double> are, mdg, eg;            // per entry: M/k + theta S, theta q^2 (M_D)_g, theta q E_g
     DevBuf<double> Fn, Fo;                  // F(t), F(tp) per step
-    DevBuf<double2> u[2], r, rh, p, v, sv, t, y, z, dinv;
+    DevBuf<double2> u[3], r, rh, p, v, sv, t, y, z, dinv, ac;
     DevBuf<double> partials, out, relres;
     DevBuf<unsigned> bar;
     DevBuf<int> status;
@@ -481,9 +481,12 @@ struct SbcArgs {
     const double* __restrict__ Fn;
     const double* __restrict__ Fo;
     double inv_k;
-    double2* u0;
+    double2* u0;              // three rotating solution levels u_{n-1}, u_n, u_{n+1}
     double2* u1;
+    double2* u2;
+    int32_t extrapolate;      // 1: initial guess 2 u_n - u_{n-1} from the second step on
     double2 *r, *rh, *p, *v, *sv, *t, *y, *z, *dinv;
+    double2* ac;              // this step's A(F) = (A_re + F^2 M_D, F E) per stored entry
     double* partials;
     unsigned* bar;
     int* status;
@@ -521,12 +524,15 @@ __device__ __forceinline__ bool sbc_reduce(double (&v)[kRedS], const SbcArgs& a,
 }
 
 // Four lanes per row: y_i = sum_j (c0 * are + c1 * mdg + c2 * m + i c3 * eg)_ij x_j
-// and, when kTwo, y2_i with the coefficients d0..d3; calls f(row, y_i, y2_i) on
-// lane 0 of each row group (every lane of the warp runs the same iterations,
-// for the shuffles).  x is written inside the launch: plain coherent loads.
+// and, when kTwo, y2_i = sum_j (d0 * are + d1 * mdg + d2 * m + i d3 * eg)_ij x2_j with
+// x2 = 2 x - xp when ext (else x); calls f(row, y_i, y2_i) on lane 0 of each row
+// group (every lane of the warp runs the same iterations, for the shuffles).  x
+// and xp are written inside the launch: plain coherent loads.
 template <bool kTwo, typename F>
-__device__ __forceinline__ void sbc_spmv(const SbcArgs& a, const double2* x, double c0, double c1, double c2,
-                                         double c3, double d0, double d1, double d2, double d3, F&& f) {
+__device__ __forceinline__ void sbc_spmv(const SbcArgs& a, const double2* x, const double2* xp, bool ext,
+                                         double c0, double c1, double c2, double c3, double d0, double d1,
+                                         double d2, double d3, F&& f) {
+    // with kTwo (phase R) the second coefficient set is A(F) = (d0 A_re + d1 M_D, d3 E), stored in ac
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -544,8 +550,14 @@ __device__ __forceinline__ void sbc_spmv(const SbcArgs& a, const double2* x, dou
                 acc.y += re * xv.y + im * xv.x;
                 if (kTwo) {
                     const double re2 = d0 * ar + d1 * md + d2 * mm, im2 = d3 * ev;
-                    acc2.x += re2 * xv.x - im2 * xv.y;
-                    acc2.y += re2 * xv.y + im2 * xv.x;
+                    double2 x2 = xv;
+                    if (ext) {
+                        const double2 xo = xp[a.col[e]];
+                        x2 = make_double2(2.0 * xv.x - xo.x, 2.0 * xv.y - xo.y);
+                    }
+                    acc2.x += re2 * x2.x - im2 * x2.y;
+                    acc2.y += re2 * x2.y + im2 * x2.x;
+                    a.ac[e] = make_double2(re2, im2);
                 }
             }
         }
@@ -562,19 +574,52 @@ __device__ __forceinline__ void sbc_spmv(const SbcArgs& a, const double2* x, dou
     }
 }
 
-__global__ void __launch_bounds__(kThreadsS) k_step_sbc(SbcArgs a) {
+// Four lanes per row: y_i = sum_j ac_ij x_j with this step's stored A(F) values;
+// calls f(row, y_i) on lane 0 of each row group.
+template <typename F>
+__device__ __forceinline__ void sbc_apply(const SbcArgs& a, const double2* x, F&& f) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int sub = lane & 3;
+    for (int64_t base = gw * 8; base < a.n; base += nw * 8) {
+        const int64_t row = base + (lane >> 2);
+        double2 acc = make_double2(0.0, 0.0);
+        if (row < a.n) {
+            const int32_t e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
+            for (int32_t e = e0 + sub; e < e1; e += 4) {
+                const double2 m = a.ac[e];
+                const double2 xv = x[a.col[e]];
+                acc.x = fma(m.x, xv.x, fma(-m.y, xv.y, acc.x));
+                acc.y = fma(m.x, xv.y, fma(m.y, xv.x, acc.y));
+            }
+        }
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        }
+        if (row < a.n && sub == 0) f(row, acc);
+    }
+}
+
+__global__ void __launch_bounds__(kThreadsS, 2) k_step_sbc(SbcArgs a) {
     __shared__ double sm[32 * kRedS];
     const unsigned nb = gridDim.x;
     unsigned gen = 0, flip = 0;
     const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t nt = (int64_t)gridDim.x * blockDim.x;
-    double2* un = a.u0;   // u_n
-    double2* ux = a.u1;   // iterate, u_{n+1} at the end of the step
+    double2* U[3] = {a.u0, a.u1, a.u2};
     for (int32_t step = 0; step < a.n_steps; ++step) {
         const double F = a.Fn[step], Fp = a.Fo[step];
-        // phase R: b = (2M/k - A_re - Fp^2 M_D - i Fp E) u_n, r = b - A(F) u_n with x0 = u_n
+        double2* un = U[step % 3];          // u_n
+        double2* um = U[(step + 2) % 3];    // u_{n-1}
+        double2* ux = U[(step + 1) % 3];    // iterate, u_{n+1} at the end of the step
+        const bool ext = a.extrapolate && step > 0;
+        // phase R: b = (2M/k - A_re - Fp^2 M_D - i Fp E) u_n, r = b - A(F) x0 with
+        // x0 = 2 u_n - u_{n-1} (or u_n)
         double red[kRedS] = {0.0, 0.0, 0.0, 0.0};
-        sbc_spmv<true>(a, un, -1.0, -Fp * Fp, 2.0 * a.inv_k, -Fp, 1.0, F * F, 0.0, F,
+        sbc_spmv<true>(a, un, um, ext, -1.0, -Fp * Fp, 2.0 * a.inv_k, -Fp, 1.0, F * F, 0.0, F,
                        [&](int64_t i, double2 b, double2 ax) {
             const double2 ri = make_double2(b.x - ax.x, b.y - ax.y);
             const int32_t d = a.diag[i];
@@ -583,7 +628,13 @@ __global__ void __launch_bounds__(kThreadsS) k_step_sbc(SbcArgs a) {
             a.rh[i] = ri;
             a.p[i] = make_double2(0.0, 0.0);
             a.v[i] = make_double2(0.0, 0.0);
-            ux[i] = un[i];
+            const double2 uc = un[i];
+            if (ext) {
+                const double2 uo = um[i];
+                ux[i] = make_double2(2.0 * uc.x - uo.x, 2.0 * uc.y - uo.y);
+            } else {
+                ux[i] = uc;
+            }
             red[0] += b.x * b.x + b.y * b.y;
             red[1] += ri.x * ri.x + ri.y * ri.y;
         });
@@ -615,7 +666,7 @@ __global__ void __launch_bounds__(kThreadsS) k_step_sbc(SbcArgs a) {
             if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return;
             // v = A y ; (rh, v)
             double r2[kRedS] = {0.0, 0.0, 0.0, 0.0};
-            sbc_spmv<false>(a, a.y, 1.0, F * F, 0.0, F, 0.0, 0.0, 0.0, 0.0, [&](int64_t i, double2 vi, double2) {
+            sbc_apply(a, a.y, [&](int64_t i, double2 vi) {
                 a.v[i] = vi;
                 const double2 c = cdotc(a.rh[i], vi);
                 r2[0] += c.x;
@@ -639,7 +690,7 @@ __global__ void __launch_bounds__(kThreadsS) k_step_sbc(SbcArgs a) {
             if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return;
             // t = A z ; (t, s), (t, t), (s, s)
             double r4[kRedS] = {0.0, 0.0, 0.0, 0.0};
-            sbc_spmv<false>(a, a.z, 1.0, F * F, 0.0, F, 0.0, 0.0, 0.0, 0.0, [&](int64_t i, double2 ti, double2) {
+            sbc_apply(a, a.z, [&](int64_t i, double2 ti) {
                 a.t[i] = ti;
                 const double2 si = a.sv[i];
                 const double2 c = cdotc(ti, si);
@@ -688,16 +739,14 @@ __global__ void __launch_bounds__(kThreadsS) k_step_sbc(SbcArgs a) {
             a.iters[step] = it;
             a.relres[step] = bb > 0.0 ? sqrt(rr / bb) : 0.0;
         }
-        double2* tmp = un;
-        un = ux;
-        ux = tmp;
-        // the next phase R gathers u_n and writes the iterate buffer
+        // the next phase R gathers u_n, u_{n-1} and writes the third buffer
         if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return;
     }
     // signal: sum_i w_i Re(u_i), total and per compartment
+    const double2* uN = U[a.n_steps % 3];
     double sg[kRedS] = {0.0, 0.0, 0.0, 0.0};
     for (int64_t i = gt; i < a.n; i += nt) {
-        const double c = a.w[i] * un[i].x;
+        const double c = a.w[i] * uN[i].x;
         sg[0] += c;
         const int rc = a.rcomp[i];
         if (rc == 0) sg[1] += c;
@@ -768,7 +817,9 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
     P.are.alloc(nnz);
     P.mdg.alloc(nnz);
     P.eg.alloc(nnz);
-    for (auto* b : {&P.u[0], &P.u[1], &P.r, &P.rh, &P.p, &P.v, &P.sv, &P.t, &P.y, &P.z, &P.dinv}) b->alloc(n);
+    for (auto* b : {&P.u[0], &P.u[1], &P.u[2], &P.r, &P.rh, &P.p, &P.v, &P.sv, &P.t, &P.y, &P.z, &P.dinv})
+        b->alloc(n);
+    P.ac.alloc(nnz);
     P.partials.alloc((size_t)2 * P.nblocks * kRedS);
     P.out.alloc(kRedS);
     P.relres.alloc(S.n_steps);
@@ -830,6 +881,8 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
         a.inv_k = 1.0 / S.dt;
         a.u0 = P.u[0];
         a.u1 = P.u[1];
+        a.u2 = P.u[2];
+        a.extrapolate = ctx->opt_fp64_extrapolate >= 1 ? 1 : 0;
         a.r = P.r;
         a.rh = P.rh;
         a.p = P.p;
@@ -839,6 +892,7 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
         a.y = P.y;
         a.z = P.z;
         a.dinv = P.dinv;
+        a.ac = P.ac;
         a.partials = P.partials;
         a.bar = P.bar;
         a.status = P.status;
@@ -864,7 +918,7 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
         float ms = 0.0f;
         BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
         stepper_ms += ms;
-        BT_CUDA(cudaMemcpyAsync(P.saved.p + (size_t)sg * n, P.u[S.n_steps % 2].p, n * sizeof(double2),
+        BT_CUDA(cudaMemcpyAsync(P.saved.p + (size_t)sg * n, P.u[S.n_steps % 3].p, n * sizeof(double2),
                                 cudaMemcpyDeviceToDevice, s));
         sig[sg] = hout[0];
         if (comp_sig)
