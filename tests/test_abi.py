@@ -37,6 +37,12 @@ def test_null_arguments_are_rejected(lib):
     assert lib.bt_adjoint_batch(None, 1, None, None, None, 1e-9, 10, 0, None, None, None, None, None) == 1
     assert lib.bt_adjoint_multi(None, 1, None, None, None, None, 1e-9, 10, 0, None, None, None, None, None) == 1
     assert lib.bt_set_kappa_mode(None, 1) == 1
+    assert lib.bt_set_periodic_mode(None, 1) == 1
+    assert lib.bt_set_schedule_integral(None, None, None, 1, 1) == 1
+    assert lib.bt_strong_periodic_info(None, None, None, None) == 1
+    assert lib.bt_adjoint_cells(None, 1.0, None, 0, None, 1e-9, 10, 0, None, None, None, None, None) == 1
+    assert lib.bt_adjoint_batch_cells(None, 1, None, None, None, None, 1e-9, 10, 0, None, None, None, None,
+                                      None) == 1
 
 
 def test_no_cpu_fallback_without_library(pkg, tmp_path, monkeypatch):
