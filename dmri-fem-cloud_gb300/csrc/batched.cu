@@ -1078,18 +1078,19 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                     const bool row_ok = row_raw < a.n;
                     const int row = row_ok ? row_raw : a.n - 1;
                     const bool mine = row_ok && lane_active;   // this lane updates its slots
-                    float2 sA[2], sx[2], sy[2], sz[2];
+                    // the lane's two slots are the Re and Im parts of one signal: one
+                    // gradient direction, so J_g = g.(Jx, Jy, Jz) is formed once per entry
+                    float2 sA[2], sJ[2];
 #pragma unroll
-                    for (int j = 0; j < 2; ++j) sA[j] = sx[j] = sy[j] = sz[j] = make_float2(0.f, 0.f);
+                    for (int j = 0; j < 2; ++j) sA[j] = sJ[j] = make_float2(0.f, 0.f);
                     const int e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
                     auto acc_entry = [&](const float4 m, const float4 zz) {
                         const float2 zj[2] = {make_float2(zz.x, zz.y), make_float2(zz.z, zz.w)};
+                        const float jg = fmaf(m.w, gz[0], fmaf(m.z, gy[0], m.y * gx[0]));
 #pragma unroll
                         for (int j = 0; j < 2; ++j) {
                             sA[j].x = fmaf(m.x, zj[j].x, sA[j].x); sA[j].y = fmaf(m.x, zj[j].y, sA[j].y);
-                            sx[j].x = fmaf(m.y, zj[j].x, sx[j].x); sx[j].y = fmaf(m.y, zj[j].y, sx[j].y);
-                            sy[j].x = fmaf(m.z, zj[j].x, sy[j].x); sy[j].y = fmaf(m.z, zj[j].y, sy[j].y);
-                            sz[j].x = fmaf(m.w, zj[j].x, sz[j].x); sz[j].y = fmaf(m.w, zj[j].y, sz[j].y);
+                            sJ[j].x = fmaf(jg, zj[j].x, sJ[j].x); sJ[j].y = fmaf(jg, zj[j].y, sJ[j].y);
                         }
                     };
                     const size_t vi = (size_t)row * Rp4 + c4;
@@ -1153,9 +1154,7 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                     float pn[4], qn[4];
 #pragma unroll
                     for (int j = 0; j < 2; ++j) {
-                        const float jr = gx[j] * sx[j].x + gy[j] * sy[j].x + gz[j] * sz[j].x;
-                        const float ji = gx[j] * sx[j].y + gy[j] * sy[j].y + gz[j] * sz[j].y;
-                        const float2 wv = make_float2(fmaf(-cn[j], ji, sA[j].x), fmaf(cn[j], jr, sA[j].y));
+                        const float2 wv = make_float2(fmaf(-cn[j], sJ[j].y, sA[j].x), fmaf(cn[j], sJ[j].x, sA[j].y));
                         const float2 bp = cmulf(beta[j], make_float2(pov[2 * j], pov[2 * j + 1]));
                         const float2 bq = cmulf(beta[j], make_float2(qov[2 * j], qov[2 * j + 1]));
                         pn[2 * j] = zov[2 * j] + bp.x;
