@@ -1072,7 +1072,10 @@ __device__ __forceinline__ void batched_body(const MixArgs& a, const unsigned bi
                 // runs the same iterations (rows past the end are clamped, converged lanes
                 // skip their own gathers and stores).
                 constexpr bool kShared = (LPR >= 8);
-                for (int g = (kShared || lane_active) ? g0 : gend; g < gend; g += gstride) {
+                // (a warp whose lanes have all converged skips the rows: nothing it
+                // would load is used)
+                const bool warp_active = __any_sync(0xffffffffu, lane_active);
+                for (int g = (kShared ? warp_active : lane_active) ? g0 : gend; g < gend; g += gstride) {
                     const int row_raw = g * G + slot;
                     if (!kShared && row_raw >= a.n) continue;
                     const bool row_ok = row_raw < a.n;
