@@ -1918,7 +1918,7 @@ static void upload_rhs(bt_ctx* ctx, SolverMixed& W, int NS, const double* q, con
 // `keep`, the final states of the last launch on this mesh; b0 is the index of
 // the batch's first signal among the mesh's signals.
 static void collect_batch(bt_ctx* ctx, SolverMixed& W, int b0, int NS, bool keep, double* sig, double* comp_sig,
-                          bt_stats* st) {
+                          bt_stats* st, const int32_t* orig = nullptr) {
     Mesh& m = ctx->mesh;
     Schedule& S = ctx->sched;
     cudaStream_t s = ctx->stream;
@@ -1935,16 +1935,20 @@ static void collect_batch(bt_ctx* ctx, SolverMixed& W, int b0, int NS, bool keep
         W.ul.download(hul.data(), hul.size(), s);
     }
     BT_CUDA(cudaStreamSynchronize(s));
+    // signal r of the batch is signal b0 + r of the call, or orig[b0 + r] when the
+    // call's signals were reordered (sig and comp_sig are then the call's arrays)
     for (int r = 0; r < NS; ++r) {
         const size_t so = (size_t)(2 * r) * (1 + kMaxCompartments);   // signal r lives in slot 2r
-        sig[r] = hsig[so];
+        const size_t o = orig ? (size_t)orig[b0 + r] : (size_t)(b0 + r);
+        const size_t oo = orig ? o : (size_t)r;                        // index into sig / comp_sig
+        sig[oo] = hsig[so];
         if (comp_sig)
-            for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)r * m.n_comp + c] = hsig[so + 1 + c];
+            for (int c = 0; c < m.n_comp; ++c) comp_sig[oo * m.n_comp + c] = hsig[so + 1 + c];
         for (int64_t i = 0; keep && i < m.n_dofs; ++i) {
             const float2 h = huh[(size_t)i * nsr + r], l = hul[(size_t)i * nsr + r];
-            W.saved[(size_t)(b0 + r) * m.n_dofs + i] = make_double2((double)h.x + l.x, (double)h.y + l.y);
+            W.saved[o * m.n_dofs + i] = make_double2((double)h.x + l.x, (double)h.y + l.y);
         }
-        for (int k = 0; k < S.n_steps; ++k) ctx->last_iters[(size_t)(b0 + r) * S.n_steps + k] = hit[k];
+        for (int k = 0; k < S.n_steps; ++k) ctx->last_iters[o * S.n_steps + k] = hit[k];
     }
     if (st) {
         for (int k = 0; k < S.n_steps; ++k) {
@@ -1985,16 +1989,34 @@ void solve_mixed(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir,
     SolverMixed& W = pack_mixed(ctx, u0, &d_u0);
     reset_stats(st, S.n_steps, rtol);
     const bool keep = keep_states(ctx, W, nsig);
+    // Signals ordered by (sequence, |q|) before they are cut into launches and warps:
+    // a launch iterates until its slowest signal converges and a warp of 32 signals
+    // until its slowest lane does, and the inner iteration count grows with q f, so
+    // signals of similar q share launches and warps (outputs keep the call's order).
+    std::vector<int32_t> ord(nsig);
+    for (int32_t i = 0; i < nsig; ++i) ord[i] = i;
+    if (ctx->opt_mixed_sort)
+        std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) {
+            const int32_t sx = seq ? seq[x] : 0, sy = seq ? seq[y] : 0;
+            if (sx != sy) return sx < sy;
+            return std::fabs(q[x]) < std::fabs(q[y]);
+        });
+    std::vector<double> qo(nsig), go((size_t)nsig * 3);
+    std::vector<int32_t> so(seq ? nsig : 0);
+    for (int32_t i = 0; i < nsig; ++i) {
+        qo[i] = q[ord[i]];
+        for (int k = 0; k < 3; ++k) go[(size_t)3 * i + k] = gdir[(size_t)3 * ord[i] + k];
+        if (seq) so[i] = seq[ord[i]];
+    }
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
     float stepper_ms = 0.0f;
     for (int32_t b0 = 0; b0 < nsig; b0 += kMaxRhs / 2) {
         const int NS = std::min<int32_t>(kMaxRhs / 2, nsig - b0);   // signals in this launch
         const int R = 2 * NS;                                        // slots: Re and Im of each
-        upload_rhs(ctx, W, NS, q + b0, gdir + 3 * b0, seq ? seq + b0 : nullptr);
+        upload_rhs(ctx, W, NS, qo.data() + b0, go.data() + 3 * b0, seq ? so.data() + b0 : nullptr);
         const auto geo = autotune_mixed(ctx, W, R, rtol, maxit, d_u0);
         stepper_ms += launch_batch(ctx, W, R, geo.lpr, geo.per_sm, geo.blocked, S.n_steps, rtol, maxit, d_u0);
-        collect_batch(ctx, W, b0, NS, keep, sig + b0, comp_sig ? comp_sig + (size_t)b0 * ctx->mesh.n_comp : nullptr,
-                      st);
+        collect_batch(ctx, W, b0, NS, keep, sig, comp_sig, st, ord.data());
         if (st) st->kernel_launches += 3;
     }
     BT_CUDA(cudaEventRecord(ctx->ev2, s));

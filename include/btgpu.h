@@ -360,8 +360,12 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *   "mixed.inner_reductions" grid-wide reductions per inner COCG iteration: 1 (the
  *                           single-reduction rearrangement) or 2 (default, the textbook form); the
  *                           adjoint's and the pseudo-periodic launches always use 2
+ *   "mixed.sort_signals"    1 (default): bt_solve's mixed path orders the signals by (sequence, |q|)
+ *                           before cutting them into launches of 256 and warps of 32, so signals of
+ *                           similar convergence share them (outputs keep the call's order); 0: as given
  *   "fp64.extrapolate"      order of the FP64 path's initial guess, extrapolated in time from the
- *                           last states: 4 (default), 3, 2, 1 (2 u_n - u_{n-1}) or 0 (u_n)
+ *                           last states: 4 (default), 3, 2, 1 (2 u_n - u_{n-1}) or 0 (u_n); the strong
+ *                           pseudo-periodic stepper uses 2 u_n - u_{n-1} for any order >= 1
  * Failure detection (every device-side wait of the persistent steppers is
  * bounded; a wait that runs out ends the launch and the call returns
  * BT_ERR_TIMEOUT, leaving the context usable):
