@@ -35,7 +35,7 @@ EXPORTS = [
     "bt_signal_noalloc", "bt_adjoint", "bt_solve_multi", "bt_set_cell_T2", "bt_tangent",
     "bt_set_schedule_phase", "bt_set_periodic", "bt_periodic_info", "bt_adjoint_batch", "bt_adjoint_multi",
     "bt_set_kappa_mode", "bt_set_schedule_integral", "bt_set_periodic_mode", "bt_strong_periodic_info",
-    "bt_adjoint_cells", "bt_adjoint_batch_cells",
+    "bt_adjoint_cells", "bt_adjoint_batch_cells", "bt_solve_dev",
 ]
 
 
@@ -118,6 +118,8 @@ def load(path=None):
                                        _D, _D, _D, _D, C.POINTER(Stats)]),
         "bt_adjoint_batch_cells": (C.c_int, [_P, C.c_int32, _D, _D, _I32, _D, C.c_double, C.c_int32, C.c_int32,
                                              _D, _D, _D, _D, C.POINTER(Stats)]),
+        "bt_solve_dev": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P, C.c_int32, C.c_double, C.c_int32, _P, _P,
+                                   C.POINTER(C.c_double), C.POINTER(Stats)]),
         "bt_tangent": (C.c_int, [_P, C.c_double, _D, C.c_int32, _D, C.c_int32, C.c_int32, C.c_int32, C.c_double,
                                  C.c_int32, _D, _D, C.POINTER(Stats)]),
         "bt_solve_multi": (C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _D, _I32, C.c_double, C.c_int32,
@@ -319,6 +321,34 @@ class Context:
                                         C.byref(st)))
         return {"signal": float(sig[0]), "dD": dD, "dinvT2": dT, "dkappa": dK.reshape(nr, nr),
                 "stats": st.as_dict()}
+
+    def solve_dev(self, q, gdir, sequence=None, u0=None, precision=PRECISION_FP64, rtol=1e-12, max_iterations=2000,
+                  compartments=False):
+        """bt_solve on device tensors: q[n], gdir[n, 3] (float64), sequence[n] (int32,
+        optional), u0[n_vertices] (float64, optional), all CUDA tensors on this
+        context's device; returns {"signal": tensor[n], "compartments": tensor[n, nc]
+        or None, "S0": float, "stats": dict} with the tensors on the same device."""
+        import torch
+
+        def dev(t, dtype):
+            if t is None:
+                return None
+            if not (torch.is_tensor(t) and t.is_cuda and t.dtype == dtype):
+                raise TypeError("solve_dev takes CUDA tensors of dtype %s" % dtype)
+            return t.contiguous()
+        q = dev(q, torch.float64)
+        n = q.numel()
+        g = dev(gdir, torch.float64).reshape(n, 3).contiguous()
+        seq = dev(sequence, torch.int32)
+        u = dev(u0, torch.float64)
+        sig = torch.empty(n, dtype=torch.float64, device=q.device)
+        comp = torch.empty((n, self.n_compartments), dtype=torch.float64, device=q.device) if compartments else None
+        S0 = C.c_double(0.0)
+        st = Stats()
+        ptr = (lambda t: None if t is None else C.c_void_p(t.data_ptr()))
+        self._check(self.lib.bt_solve_dev(self.h, n, ptr(q), ptr(g), ptr(seq), ptr(u), int(precision), float(rtol),
+                                          int(max_iterations), ptr(sig), ptr(comp), C.byref(S0), C.byref(st)))
+        return {"signal": sig, "compartments": comp, "S0": S0.value, "stats": st.as_dict()}
 
     def adjoint_cells(self, q, gdir, sequence=0, u0=None, rtol=1e-13, max_iterations=5000, stride=0):
         """Signal and its derivatives (unnormalised) w.r.t. a per-cell diffusion

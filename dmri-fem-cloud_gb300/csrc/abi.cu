@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <vector>
 
 namespace bt {
 void free_solver64(bt_ctx* ctx);
@@ -405,6 +406,68 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
                 *S0_out = ctx->mesh.volume;
             }
         }
+    });
+}
+
+// Device-pointer variant of bt_solve: the per-signal parameters and u0 are read
+// from device memory (staged through the host, where the solve validates them and
+// builds its schedule), the signals are written to device memory on the
+// context's stream.
+static bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+int bt_solve_dev(bt_ctx* ctx, int32_t n_signals, const double* d_q, const double* d_gdir, const int32_t* d_sequence,
+                 const double* d_u0, int32_t precision, double rtol, int32_t max_iterations, double* d_signal_out,
+                 double* d_compartment_out, double* S0_out, bt_stats* stats) {
+    if (!ctx) return BT_ERR_INVALID;
+    std::vector<double> q, g, u0, sig, comp;
+    std::vector<int32_t> seq;
+    int rc = guarded(ctx, [&] {
+        BT_REQUIRE(ctx->mesh.built, BT_ERR_STATE, "bt_solve_dev: no mesh");
+        BT_REQUIRE(n_signals >= 1 && d_q && d_gdir && d_signal_out, BT_ERR_INVALID, "bt_solve_dev: bad arguments");
+        use_device(ctx);
+        for (const void* p : {(const void*)d_q, (const void*)d_gdir, (const void*)d_signal_out})
+            BT_REQUIRE(is_device_ptr(p), BT_ERR_INVALID, "bt_solve_dev: q, gdir and signal_out must be device pointers");
+        BT_REQUIRE(!d_sequence || is_device_ptr(d_sequence), BT_ERR_INVALID, "bt_solve_dev: sequence must be a device pointer");
+        BT_REQUIRE(!d_u0 || is_device_ptr(d_u0), BT_ERR_INVALID, "bt_solve_dev: u0 must be a device pointer");
+        BT_REQUIRE(!d_compartment_out || is_device_ptr(d_compartment_out), BT_ERR_INVALID,
+                   "bt_solve_dev: compartment_out must be a device pointer");
+        cudaStream_t s = ctx->stream;
+        q.resize(n_signals);
+        g.resize((size_t)3 * n_signals);
+        BT_CUDA(cudaMemcpyAsync(q.data(), d_q, q.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        BT_CUDA(cudaMemcpyAsync(g.data(), d_gdir, g.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (d_sequence) {
+            seq.resize(n_signals);
+            BT_CUDA(cudaMemcpyAsync(seq.data(), d_sequence, seq.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        }
+        if (d_u0) {
+            u0.resize(ctx->mesh.n_v);
+            BT_CUDA(cudaMemcpyAsync(u0.data(), d_u0, u0.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        BT_CUDA(cudaStreamSynchronize(s));
+        sig.resize(n_signals);
+        comp.resize((size_t)n_signals * ctx->mesh.n_comp);
+    });
+    if (rc != BT_OK) return rc;
+    rc = bt_solve(ctx, n_signals, q.data(), g.data(), d_sequence ? seq.data() : nullptr, d_u0 ? u0.data() : nullptr,
+                  precision, rtol, max_iterations, sig.data(), d_compartment_out ? comp.data() : nullptr, S0_out,
+                  stats);
+    if (rc != BT_OK) return rc;
+    return guarded(ctx, [&] {
+        cudaStream_t s = ctx->stream;
+        BT_CUDA(cudaMemcpyAsync(d_signal_out, sig.data(), sig.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (d_compartment_out)
+            BT_CUDA(cudaMemcpyAsync(d_compartment_out, comp.data(), comp.size() * sizeof(double),
+                                    cudaMemcpyHostToDevice, s));
+        BT_CUDA(cudaStreamSynchronize(s));   // the host staging buffers go out of scope
     });
 }
 

@@ -243,6 +243,20 @@ int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir
              double rtol, int32_t max_iterations, double* signal_out,
              double* compartment_out, double* S0_out, bt_stats* stats);
 
+/* bt_solve with device pointers (torch CUDA tensors, ...): d_q[n_signals],
+ * d_gdir[n_signals*3], d_sequence[n_signals] (nullable), d_u0[n_vertices]
+ * (nullable) are read from device memory and d_signal_out[n_signals],
+ * d_compartment_out[n_signals*n_compartments] (nullable) written to it, on the
+ * context's stream; S0_out and stats stay host pointers.  The per-signal
+ * parameters and u0 are staged through the host (the solve validates them and
+ * builds its schedule there); the caller keeps the arrays alive for the call,
+ * which returns after the outputs are written.  Non-device pointers are
+ * rejected (BT_ERR_INVALID). */
+int bt_solve_dev(bt_ctx* ctx, int32_t n_signals, const double* d_q, const double* d_gdir,
+                 const int32_t* d_sequence, const double* d_u0, int32_t precision, double rtol,
+                 int32_t max_iterations, double* d_signal_out, double* d_compartment_out, double* S0_out,
+                 bt_stats* stats);
+
 /* Several meshes in one persistent launch (mixed precision): mesh m is the
  * mesh, coefficients, assembly and schedule of contexts[m] and gets
  * n_signals[m] (1..256) signals; q, gdir, sequence and signal_out list the

@@ -43,6 +43,7 @@ def test_null_arguments_are_rejected(lib):
     assert lib.bt_adjoint_cells(None, 1.0, None, 0, None, 1e-9, 10, 0, None, None, None, None, None) == 1
     assert lib.bt_adjoint_batch_cells(None, 1, None, None, None, None, 1e-9, 10, 0, None, None, None, None,
                                       None) == 1
+    assert lib.bt_solve_dev(None, 1, None, None, None, None, 0, 1e-9, 10, None, None, None, None) == 1
 
 
 def test_no_cpu_fallback_without_library(pkg, tmp_path, monkeypatch):

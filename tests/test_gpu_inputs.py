@@ -206,3 +206,36 @@ def test_adjoint_fd_on_the_48_layered_sphere(pkg, lib):
     fd = (sig(D, iT2, Kp) - sig(D, iT2, Km)) / (2 * h * kp[i, j])
     assert abs(adj["dkappa"][i, j] - fd) <= ADJ_RTOL * abs(fd), ("kappa", adj["dkappa"][i, j], fd)
     ctx.close()
+
+
+def test_device_pointer_solve(pkg, lib):
+    """bt_solve_dev with torch CUDA tensors (q, gdir, sequence, u0 in, signals out)
+    gives bt_solve's signals bit for bit; host arrays are refused."""
+    import torch
+    xyz, tets = pkg.meshgen.kuhn_box(-5, 5, 8)
+    reg = pkg.meshgen.cylinder_regions(xyz, tets, [(0.0, 0.0)], [3.0])
+    ctx = pkg.Context(0)
+    ctx.mesh_upload(xyz, tets, reg, 2)
+    ctx.set_coefficients([3e-3, 2e-3], None, 1e-5)
+    ctx.assemble()
+    seqs = [pkg.sequences.pgse(1000.0, 3000.0), pkg.sequences.cos_ogse(1000.0, 3000.0)]
+    fns, fos = zip(*[pkg.sequences.profile_samples(p, 50.0) for p in seqs])
+    ctx.set_schedule(np.array(fns), np.array(fos), 50.0)
+    q = np.array([pkg.sequences.b_to_q(b, seqs[0].int4gb()) for b in (500.0, 1500.0, 3000.0)])
+    g = np.array([[1.0, 0.0, 0.0], [0.0, 0.6, 0.8], [0.48, 0.6, 0.64]])
+    sq = np.array([0, 1, 0], np.int32)
+    u0 = 1.0 + 0.1 * np.sin(xyz[:, 0])
+    for prec in (pkg.PRECISION_FP64, pkg.PRECISION_MIXED):
+        ref = ctx.solve(q, g, sq, u0, prec, 1e-12 if prec == pkg.PRECISION_FP64 else 1e-9, 20000, compartments=True)
+        out = ctx.solve_dev(torch.tensor(q, device="cuda"), torch.tensor(g, device="cuda"),
+                            torch.tensor(sq, device="cuda"), torch.tensor(u0, device="cuda"), prec,
+                            1e-12 if prec == pkg.PRECISION_FP64 else 1e-9, 20000, compartments=True)
+        assert out["signal"].is_cuda
+        assert np.array_equal(out["signal"].cpu().numpy(), ref["signal"])
+        assert np.array_equal(out["compartments"].cpu().numpy(), ref["compartments"])
+        assert out["S0"] == ref["S0"]
+    # host memory is refused
+    rc = lib.bt_solve_dev(ctx.h, 1, q.ctypes.data, g.ctypes.data, None, None, 0, 1e-9, 100,
+                          torch.zeros(1, dtype=torch.float64, device="cuda").data_ptr(), None, None, None)
+    assert rc == 1
+    ctx.close()
