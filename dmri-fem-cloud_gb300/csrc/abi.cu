@@ -3,6 +3,8 @@
 // the context; nothing here calls exit().
 #include "bt_common.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -14,6 +16,15 @@ void free_solver_mixed(bt_ctx* ctx);
 }  // namespace bt
 
 namespace {
+
+// NVTX range around an entry point (visible in Nsight Systems / ncu range filters;
+// a no-op without an attached tool).
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 
 template <typename F>
 int guarded(bt_ctx* ctx, F&& f) {
@@ -112,6 +123,7 @@ int bt_set_stream(bt_ctx* ctx, void* cuda_stream) {
 
 int bt_mesh_upload(bt_ctx* ctx, const double* xyz, int64_t n_vertices, const int32_t* tets, int64_t n_cells,
                    const int32_t* cell_region, int32_t n_regions, const int32_t* region_compartment) {
+    Range range_("bt_mesh_upload");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(xyz && tets && cell_region, BT_ERR_INVALID, "bt_mesh_upload: NULL array");
@@ -233,6 +245,7 @@ int bt_set_cell_T2(bt_ctx* ctx, const double* invT2_cell) {
 }
 
 int bt_assemble(bt_ctx* ctx) {
+    Range range_("bt_assemble");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         use_device(ctx);
@@ -314,6 +327,7 @@ static void apply_periodic(bt_ctx* ctx, const int32_t* dir) {
 }
 
 int bt_set_periodic(bt_ctx* ctx, const int32_t* periodic_dir) {
+    Range range_("bt_set_periodic");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built, BT_ERR_STATE, "bt_set_periodic: no mesh");
@@ -362,6 +376,7 @@ int bt_periodic_info(bt_ctx* ctx, bt_periodic_info_t* out) {
 int bt_solve(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir, const int32_t* sequence,
              const double* u0, int32_t precision, double rtol, int32_t max_iterations, double* signal_out,
              double* compartment_out, double* S0_out, bt_stats* stats) {
+    Range range_("bt_solve");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_solve: mesh not assembled");
@@ -426,6 +441,7 @@ static bool is_device_ptr(const void* p) {
 int bt_solve_dev(bt_ctx* ctx, int32_t n_signals, const double* d_q, const double* d_gdir, const int32_t* d_sequence,
                  const double* d_u0, int32_t precision, double rtol, int32_t max_iterations, double* d_signal_out,
                  double* d_compartment_out, double* S0_out, bt_stats* stats) {
+    Range range_("bt_solve_dev");
     if (!ctx) return BT_ERR_INVALID;
     std::vector<double> q, g, u0, sig, comp;
     std::vector<int32_t> seq;
@@ -474,6 +490,7 @@ int bt_solve_dev(bt_ctx* ctx, int32_t n_signals, const double* d_q, const double
 int bt_solve_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_signals, const double* q,
                    const double* gdir, const int32_t* sequence, double rtol, int32_t max_iterations,
                    double* signal_out, double* S0_out, bt_stats* stats) {
+    Range range_("bt_solve_multi");
     if (!contexts || n_meshes < 1 || !contexts[0]) return BT_ERR_INVALID;
     bt_ctx* c0 = contexts[0];
     return guarded(c0, [&] {
@@ -522,6 +539,7 @@ int bt_solve_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n_s
 int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0, int32_t param,
                int32_t i, int32_t j, double rtol, int32_t max_iterations, double* signal_out, double* dsignal_out,
                bt_stats* stats) {
+    Range range_("bt_tangent");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_tangent: mesh not assembled");
@@ -543,6 +561,7 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
 int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0, double rtol,
                int32_t max_iterations, int32_t checkpoint_stride, double* signal_out, double* dS_dD,
                double* dS_dinvT2, double* dS_dkappa, bt_stats* stats) {
+    Range range_("bt_adjoint");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint: mesh not assembled");
@@ -566,6 +585,7 @@ int bt_adjoint(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
 int bt_adjoint_cells(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, const double* u0, double rtol,
                      int32_t max_iterations, int32_t checkpoint_stride, double* signal_out, double* dS_dD_cell,
                      double* dS_dinvT2_cell, double* dS_dkappa, bt_stats* stats) {
+    Range range_("bt_adjoint_cells");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint_cells: mesh not assembled");
@@ -590,6 +610,7 @@ int bt_adjoint_cells(bt_ctx* ctx, double q, const double* gdir, int32_t sequence
 int bt_adjoint_batch(bt_ctx* ctx, int32_t n_signals, const double* q, const double* gdir, const int32_t* sequence,
                      double rtol, int32_t max_iterations, int32_t checkpoint_stride, double* signal_out,
                      double* dS_dD, double* dS_dinvT2, double* dS_dkappa, bt_stats* stats) {
+    Range range_("bt_adjoint_batch");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint_batch: mesh not assembled");
@@ -614,6 +635,7 @@ int bt_adjoint_batch_cells(bt_ctx* ctx, int32_t n_signals, const double* q, cons
                            const int32_t* sequence, const double* weights, double rtol, int32_t max_iterations,
                            int32_t checkpoint_stride, double* signal_out, double* dS_dD_cell, double* dS_dinvT2_cell,
                            double* dS_dkappa, bt_stats* stats) {
+    Range range_("bt_adjoint_batch_cells");
     if (!ctx) return BT_ERR_INVALID;
     return guarded(ctx, [&] {
         BT_REQUIRE(ctx->mesh.built && ctx->mat.done, BT_ERR_STATE, "bt_adjoint_batch_cells: mesh not assembled");
@@ -639,6 +661,7 @@ int bt_adjoint_multi(bt_ctx* const* contexts, int32_t n_meshes, const int32_t* n
                      const double* gdir, const int32_t* sequence, double rtol, int32_t max_iterations,
                      int32_t checkpoint_stride, double* signal_out, double* dS_dD, double* dS_dinvT2,
                      double* dS_dkappa, bt_stats* stats) {
+    Range range_("bt_adjoint_multi");
     if (!contexts || n_meshes < 1 || !contexts[0]) return BT_ERR_INVALID;
     bt_ctx* c0 = contexts[0];
     return guarded(c0, [&] {
