@@ -270,6 +270,9 @@ def _context(pkg, w, local, stream):
     return ctx, np.array(fns), np.array(fos)
 
 
+NOMINAL_HBM_GBS = 7900.0   # GB300 HBM3e nominal, for reference beside the measured copy bandwidth
+
+
 def roofline_fp64(info, st, n_sig, peak, peak_src, traffic):
     iters = st["total_iterations"] / n_sig
     byts = alg_bytes_fp64(info["n_dofs"], info["nnz"], st["steps"], iters)
@@ -278,7 +281,8 @@ def roofline_fp64(info, st, n_sig, peak, peak_src, traffic):
     out = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
            "traffic": traffic.get("bytes_per_launch") if traffic else None,
            "kernel": "k_step64 (persistent FP64 CN/COCG stepper, one launch per signal)",
-           "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src}
+           "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src,
+           "frac_of_nominal_7900": ach / NOMINAL_HBM_GBS}
     if traffic:
         out["note"] = ("L2-resident: ncu counts %.0f MB of DRAM traffic per launch, %.3f%% of the %.0f GB of "
                        "algorithmic bytes, so `achieved` counts L2-served bytes and `frac` is not an HBM "
@@ -442,7 +446,8 @@ def mixed_cfg2_leg(args, pkg, ctx, q, g, pidx, n64, ms64, gold, sel, traffic, in
     roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
             "traffic": traffic.get("bytes_per_launch") if traffic else None,
             "kernel": "k_batched (persistent mixed-precision stepper, %d signals per launch)" % n_sig,
-            "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src}
+            "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src,
+           "frac_of_nominal_7900": ach / NOMINAL_HBM_GBS}
     if traffic:
         roof["note"] = ("L2-resident: ncu counts %.0f MB of DRAM traffic per launch, %.2f%% of the algorithmic "
                         "bytes; `frac` counts L2-served bytes" % (traffic["bytes_per_launch"] / 1e6,
@@ -513,6 +518,7 @@ def batched_leg(args, pkg, stream, flush, peak, peak_src, traffic):
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                          "traffic": tr.get("bytes_per_launch") if tr else None,
                          "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src,
+                         "frac_of_nominal_7900": ach / NOMINAL_HBM_GBS,
                          "note": "algorithmic bytes (bench.alg_bytes_mixed); working set %.1f GB, %.0fx the L2"
                                  % (wset / 1e9, wset / L2_BYTES)}}
 
