@@ -83,3 +83,30 @@ def test_cli_run_matches_oracle(pkg, lib, tmp_path):
     assert abs(got - ref.normalized) <= 6e-7 * abs(ref.normalized), (got, ref.normalized)   # 7 printed digits
     log = (tmp_path / "log.txt").read_text()
     assert "Normalized signal: %.6e" % got in log and "kappa: 3.000e-05" in log
+
+
+@pytest.mark.gpu
+def test_cli_strong_periodic_matches_oracle(pkg, lib, tmp_path):
+    """-IsPeriodic 1 with -pdir: the strong pseudo-periodic form through the
+    command line, against the oracle's folded system."""
+    from oracle import strong
+    xyz, tets = pkg.meshgen.kuhn_box(-5, 5, 6)
+    X = xyz[tets]
+    c = 0.5 * (X.min(axis=1) + X.max(axis=1))
+    reg = (c[:, 0] ** 2 + c[:, 1] ** 2 < 2.6 ** 2).astype(np.int32)   # cylinder on whole cubes
+    tags = np.where(reg == 1, 3, 2)
+    mesh = tmp_path / "box.msh"
+    pkg.meshfiles.write_msh2(mesh, xyz, tets, tags)
+    argv = [sys.executable, os.path.join(ROOT, "dmri-fem-cloud_gb300", "cli.py"), "-f", str(mesh), "-M", "1",
+            "-IsPeriodic", "1", "-pdir", "1", "1", "1", "-b", "1500", "-p", "2e-5", "-K", "3e-3",
+            "-gdir", "0.6", "0.8", "0", "-k", "200"]
+    r = subprocess.run(argv, capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr
+    m = re.search(r"Normalized signal: ([0-9.eE+-]+)", r.stdout)
+    assert m, r.stdout
+    got = float(m.group(1))
+    prof = oracle.PGSE(10600, 43100)
+    q = oracle.bvalue_to_q(1500.0, prof.int4gb())
+    sd = strong.duplicated_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 1], (0.6, 0.8, 0.0))
+    ref = strong.solve_strong(sd, prof, q, 200.0)
+    assert abs(got - ref["normalized"]) <= 6e-7 * abs(ref["normalized"]), (got, ref["normalized"])
