@@ -745,6 +745,9 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
             BT_REQUIRE(iv == 1 || iv == 2, BT_ERR_INVALID, "mixed.inner_reductions must be 1 or 2");
             ctx->opt_mixed_inner = iv;
             bt::reset_tuning_mixed(ctx);
+        } else if (k == "strong.batch") {
+            BT_REQUIRE(iv == 0 || iv == 1, BT_ERR_INVALID, "strong.batch must be 0 or 1");
+            ctx->opt_strong_batch = iv;
         } else if (k == "mixed.sort_signals") {
             BT_REQUIRE(iv == 0 || iv == 1, BT_ERR_INVALID, "mixed.sort_signals must be 0 or 1");
             ctx->opt_mixed_sort = iv;

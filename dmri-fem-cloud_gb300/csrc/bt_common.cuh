@@ -212,6 +212,7 @@ struct bt_ctx {
     int opt_fp64_extrapolate = 4;    // order of the FP64 path's extrapolated initial guess (0..4)
     int opt_mixed_inner = 2;          // grid-wide reductions per inner COCG iteration: 1 or 2
     int opt_mixed_sort = 1;           // order a solve's signals by (sequence, |q|) before batching
+    int opt_strong_batch = 1;         // strong form: signals of one direction share a batched launch
     // failure detection: time limit of every device-side wait, and a switch that
     // makes the next solve's first wait run out (see stalled_wait)
     unsigned long long opt_wait_ns = 2000000000ull;

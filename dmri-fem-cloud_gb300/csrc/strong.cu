@@ -46,6 +46,7 @@
 #include <array>
 #include <cmath>
 #include <map>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -74,6 +75,10 @@ struct Strong {
     DevBuf<int32_t> iters;
     DevBuf<double2> saved;
     int32_t saved_nsig = 0;
+    // batched stepper (several signals of one gradient direction): vectors [row][32]
+    int32_t mblocks = 0;
+    DevBuf<double2> mu[3], mr, mrh, mp, mv, ms, mt, my, mz, mdinv;
+    DevBuf<double> mq, mFn, mFo, mpart, mfin, mout, mrel;
 };
 
 namespace {
@@ -760,6 +765,293 @@ __global__ void __launch_bounds__(kThreadsS, 2) k_step_sbc(SbcArgs a) {
     }
 }
 
+// ----------------------------------------------------- batched stepper --
+// Up to 32 signals of one gradient direction in one cooperative launch: a warp
+// takes a row, its lane l the row's value of signal l, so each stored entry
+// (column, A_re, M_D, E of the unit-q pack) is read once for all of them and a
+// signal's coefficients q^2 F^2 and q F multiply per lane.  Every signal runs its
+// own Jacobi-BiCGSTAB (its own rho, alpha, omega; a converged signal stops
+// moving) and the launch iterates until all have converged.  Sums over rows go
+// per signal through two-stage grid reductions (block partials; one warp per
+// value over the blocks; the results read by every block), fixed order.
+constexpr int kMR = 32;   // signals per batched launch (lanes)
+constexpr int kMV = 4;    // values per signal in one reduction
+
+struct SbcMultiArgs {
+    int64_t n;
+    const int32_t* __restrict__ row_ptr;
+    const int32_t* __restrict__ col;
+    const int32_t* __restrict__ diag;
+    const int32_t* __restrict__ rcomp;
+    const double* __restrict__ m;
+    const double* __restrict__ are;
+    const double* __restrict__ md;   // theta (M_D)_g of unit q
+    const double* __restrict__ ev;   // theta E_g of unit q
+    const double* __restrict__ w;
+    const double* __restrict__ q;    // [kMR]
+    const double* __restrict__ Fn;   // [kMR][n_steps]
+    const double* __restrict__ Fo;
+    double inv_k;
+    int32_t R, n_steps, maxit, extrapolate;
+    double rtol2;
+    double2 *u0, *u1, *u2, *r, *rh, *p, *v, *sv, *t, *y, *z, *dinv;   // [n][kMR]
+    double* partials;                // [2][nb][kMR * kMV]
+    double* fin;                     // [kMR * kMV]
+    unsigned* bar;
+    int* status;
+    int32_t* iters;                  // [n_steps]
+    double* relres;                  // [kMR][n_steps]
+    double* out;                     // [kMR][3]
+    unsigned long long wait_ns;
+};
+
+// Per-signal sums: v[k] of this lane (its signal) summed over every row-warp of
+// the grid; on return v holds the totals (every lane of every block).
+__device__ __forceinline__ bool sbcm_reduce(double (&v)[kMV], const SbcMultiArgs& a, unsigned nb, unsigned& flip,
+                                            unsigned& gen, double* sm /* [kWarps * kMR * kMV] */) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    constexpr int V = kMR * kMV;
+#pragma unroll
+    for (int k = 0; k < kMV; ++k) sm[(wid * kMR + lane) * kMV + k] = v[k];
+    __syncthreads();
+    double* P = a.partials + (size_t)(flip & 1u) * nb * V;
+    ++flip;
+    for (int t = threadIdx.x; t < V; t += blockDim.x) {
+        double s = 0.0;
+        for (int w = 0; w < nw; ++w) s += sm[w * V + t];
+        P[(size_t)blockIdx.x * V + t] = s;
+    }
+    if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return false;
+    // stage 2: warp gw of the grid sums value gw over the blocks
+    const unsigned gw = blockIdx.x * nw + wid;
+    for (unsigned t = gw; t < (unsigned)V; t += nb * nw) {
+        double s = 0.0;
+        for (unsigned b = lane; b < nb; b += 32) s += __ldcg(&P[(size_t)b * V + t]);
+        s = warp_sum(s);
+        if (lane == 0) a.fin[t] = s;
+    }
+    if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return false;
+#pragma unroll
+    for (int k = 0; k < kMV; ++k) v[k] = __ldcg(&a.fin[lane * kMV + k]);
+    __syncthreads();
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreadsS, 1) k_step_sbc_multi(SbcMultiArgs a) {
+    __shared__ double sm[(kThreadsS / 32) * kMR * kMV];
+    const unsigned nb = gridDim.x;
+    unsigned gen = 0, flip = 0;
+    const int lane = threadIdx.x & 31;
+    const bool live = lane < a.R;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const double ql = live ? a.q[lane] : 0.0;
+    double2* U[3] = {a.u0, a.u1, a.u2};
+    int its_total = 0;
+    (void)its_total;
+    for (int32_t step = 0; step < a.n_steps; ++step) {
+        const double F = live ? a.Fn[(size_t)lane * a.n_steps + step] : 0.0;
+        const double Fp = live ? a.Fo[(size_t)lane * a.n_steps + step] : 0.0;
+        const double c2 = ql * ql * F * F, c1 = ql * F, p2 = ql * ql * Fp * Fp, p1 = ql * Fp;
+        double2* un = U[step % 3];
+        double2* um = U[(step + 2) % 3];
+        double2* ux = U[(step + 1) % 3];
+        const bool ext = a.extrapolate && step > 0;
+        // phase R: b = (2M/k - A_re - Fp^2 q^2 M_D - i Fp q E) u_n, x0 = 2 u_n - u_{n-1},
+        // r = b - A(F) x0, Jacobi inverse
+        double red[kMV] = {0.0, 0.0, 0.0, 0.0};
+        for (int64_t row = gw; row < a.n; row += nwarps) {
+            const size_t vi = (size_t)row * kMR + lane;
+            double2 b = make_double2(0.0, 0.0), ax = make_double2(0.0, 0.0);
+            const int32_t e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
+            for (int32_t e = e0; e < e1; ++e) {
+                const size_t cj = (size_t)a.col[e] * kMR + lane;
+                const double ar = a.are[e], mdv = a.md[e], mm = a.m[e], evv = a.ev[e];
+                const double2 xv = un[cj];
+                double2 x0 = xv;
+                if (ext) {
+                    const double2 xo = um[cj];
+                    x0 = make_double2(2.0 * xv.x - xo.x, 2.0 * xv.y - xo.y);
+                }
+                const double rb = 2.0 * a.inv_k * mm - ar - p2 * mdv, ib = -p1 * evv;
+                b.x += rb * xv.x - ib * xv.y;
+                b.y += rb * xv.y + ib * xv.x;
+                const double ra = ar + c2 * mdv, ia = c1 * evv;
+                ax.x += ra * x0.x - ia * x0.y;
+                ax.y += ra * x0.y + ia * x0.x;
+            }
+            const int32_t d = a.diag[row];
+            const double2 ri = make_double2(b.x - ax.x, b.y - ax.y);
+            a.dinv[vi] = cinv(make_double2(a.are[d] + c2 * a.md[d], c1 * a.ev[d]));
+            a.r[vi] = ri;
+            a.rh[vi] = ri;
+            a.p[vi] = make_double2(0.0, 0.0);
+            a.v[vi] = make_double2(0.0, 0.0);
+            const double2 uc = un[vi];
+            if (ext) {
+                const double2 uo = um[vi];
+                ux[vi] = make_double2(2.0 * uc.x - uo.x, 2.0 * uc.y - uo.y);
+            } else {
+                ux[vi] = uc;
+            }
+            red[0] += b.x * b.x + b.y * b.y;
+            red[1] += ri.x * ri.x + ri.y * ri.y;
+        }
+        if (!sbcm_reduce(red, a, nb, flip, gen, sm)) return;
+        const double bb = red[0], tol2 = a.rtol2 * red[0];
+        double rr = red[1];
+        bool act = live && rr > tol2;
+        double2 rho = make_double2(rr, 0.0), rho_old = make_double2(1.0, 0.0);
+        double2 alpha = make_double2(1.0, 0.0), omega = make_double2(1.0, 0.0);
+        bool first = true;
+        int it = 0;
+        while (__syncthreads_or(act)) {   // the same in every block: the sums are grid-identical
+            if (it >= a.maxit) {
+                if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
+                return;
+            }
+            if (act && rho.x == 0.0 && rho.y == 0.0) {
+                atomicCAS(a.status, DEV_OK, DEV_BREAKDOWN);
+                act = false;
+            }
+            // p = r + beta (p - omega v), y = D^-1 p
+            const double2 beta = first ? make_double2(0.0, 0.0) : cmul(cdiv(rho, rho_old), cdiv(alpha, omega));
+            first = false;
+            if (act)
+                for (int64_t row = gw; row < a.n; row += nwarps) {
+                    const size_t vi = (size_t)row * kMR + lane;
+                    const double2 pv = a.p[vi], vv = a.v[vi], rv = a.r[vi];
+                    const double2 pw = make_double2(pv.x - (omega.x * vv.x - omega.y * vv.y),
+                                                    pv.y - (omega.x * vv.y + omega.y * vv.x));
+                    const double2 bp = cmul(beta, pw);
+                    const double2 pn = make_double2(rv.x + bp.x, rv.y + bp.y);
+                    a.p[vi] = pn;
+                    a.y[vi] = cmul(a.dinv[vi], pn);
+                }
+            if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return;
+            // v = A y ; (rh, v)
+            double r2[kMV] = {0.0, 0.0, 0.0, 0.0};
+            if (act)
+                for (int64_t row = gw; row < a.n; row += nwarps) {
+                    const size_t vi = (size_t)row * kMR + lane;
+                    double2 acc = make_double2(0.0, 0.0);
+                    for (int32_t e = a.row_ptr[row]; e < a.row_ptr[row + 1]; ++e) {
+                        const double ra = a.are[e] + c2 * a.md[e], ia = c1 * a.ev[e];
+                        const double2 xv = a.y[(size_t)a.col[e] * kMR + lane];
+                        acc.x += ra * xv.x - ia * xv.y;
+                        acc.y += ra * xv.y + ia * xv.x;
+                    }
+                    a.v[vi] = acc;
+                    const double2 c = cdotc(a.rh[vi], acc);
+                    r2[0] += c.x;
+                    r2[1] += c.y;
+                }
+            if (!sbcm_reduce(r2, a, nb, flip, gen, sm)) return;
+            const double2 rv = make_double2(r2[0], r2[1]);
+            if (act && rv.x == 0.0 && rv.y == 0.0) {
+                atomicCAS(a.status, DEV_OK, DEV_BREAKDOWN);
+                act = false;
+            }
+            if (act) alpha = cdiv(rho, rv);
+            // s = r - alpha v ; z = D^-1 s
+            if (act)
+                for (int64_t row = gw; row < a.n; row += nwarps) {
+                    const size_t vi = (size_t)row * kMR + lane;
+                    const double2 av = cmul(alpha, a.v[vi]), rv2 = a.r[vi];
+                    const double2 si = make_double2(rv2.x - av.x, rv2.y - av.y);
+                    a.sv[vi] = si;
+                    a.z[vi] = cmul(a.dinv[vi], si);
+                }
+            if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return;
+            // t = A z ; (t, s), (t, t), (s, s)
+            double r4[kMV] = {0.0, 0.0, 0.0, 0.0};
+            if (act)
+                for (int64_t row = gw; row < a.n; row += nwarps) {
+                    const size_t vi = (size_t)row * kMR + lane;
+                    double2 acc = make_double2(0.0, 0.0);
+                    for (int32_t e = a.row_ptr[row]; e < a.row_ptr[row + 1]; ++e) {
+                        const double ra = a.are[e] + c2 * a.md[e], ia = c1 * a.ev[e];
+                        const double2 xv = a.z[(size_t)a.col[e] * kMR + lane];
+                        acc.x += ra * xv.x - ia * xv.y;
+                        acc.y += ra * xv.y + ia * xv.x;
+                    }
+                    a.t[vi] = acc;
+                    const double2 si = a.sv[vi];
+                    const double2 c = cdotc(acc, si);
+                    r4[0] += c.x;
+                    r4[1] += c.y;
+                    r4[2] += acc.x * acc.x + acc.y * acc.y;
+                    r4[3] += si.x * si.x + si.y * si.y;
+                }
+            if (!sbcm_reduce(r4, a, nb, flip, gen, sm)) return;
+            ++it;
+            // this signal's s is already small enough (or t vanished): x += alpha y, r = s, done
+            const bool early = act && (r4[3] <= tol2 || r4[2] == 0.0);
+            if (act) omega = early ? make_double2(0.0, 0.0) : make_double2(r4[0] / r4[2], r4[1] / r4[2]);
+            // x += alpha y + omega z ; r = s - omega t ; (rh, r), (r, r)
+            double r3[kMV] = {0.0, 0.0, 0.0, 0.0};
+            if (act)
+                for (int64_t row = gw; row < a.n; row += nwarps) {
+                    const size_t vi = (size_t)row * kMR + lane;
+                    const double2 ay = cmul(alpha, a.y[vi]), oz = cmul(omega, a.z[vi]), ot = cmul(omega, a.t[vi]);
+                    const double2 xv = ux[vi], si = a.sv[vi];
+                    ux[vi] = make_double2(xv.x + ay.x + oz.x, xv.y + ay.y + oz.y);
+                    const double2 rn = make_double2(si.x - ot.x, si.y - ot.y);
+                    a.r[vi] = rn;
+                    const double2 c = cdotc(a.rh[vi], rn);
+                    r3[0] += c.x;
+                    r3[1] += c.y;
+                    r3[2] += rn.x * rn.x + rn.y * rn.y;
+                }
+            if (!sbcm_reduce(r3, a, nb, flip, gen, sm)) return;
+            if (act) {
+                rho_old = rho;
+                rho = make_double2(r3[0], r3[1]);
+                rr = r3[2];
+                if (early || rr <= tol2) act = false;
+                else if (omega.x == 0.0 && omega.y == 0.0) {
+                    atomicCAS(a.status, DEV_OK, DEV_BREAKDOWN);
+                    act = false;
+                }
+            }
+        }
+        if (blockIdx.x == 0 && threadIdx.x < 32) {
+            if (threadIdx.x == 0) a.iters[step] = it;
+            if (live) a.relres[(size_t)lane * a.n_steps + step] = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+        }
+        if (!grid_barrier(a.bar, nb, a.status, gen, a.wait_ns)) return;
+    }
+    // signals: sum_i w_i Re(u_i), total and per compartment
+    const double2* uN = U[a.n_steps % 3];
+    double sg[kMV] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t row = gw; row < a.n; row += nwarps) {
+        const double c = a.w[row] * uN[(size_t)row * kMR + lane].x;
+        sg[0] += c;
+        const int rc = a.rcomp[row];
+        if (rc == 0) sg[1] += c;
+        else if (rc == 1) sg[2] += c;
+    }
+    if (!sbcm_reduce(sg, a, nb, flip, gen, sm)) return;
+    if (blockIdx.x == 0 && threadIdx.x < 32 && live) {
+        a.out[lane * 3 + 0] = sg[0];
+        a.out[lane * 3 + 1] = sg[1];
+        a.out[lane * 3 + 2] = sg[2];
+    }
+}
+
+// Initial state of every lane of the batched stepper, and the lane -> signal
+// copy of the final states.
+__global__ void k_sbcm_init(int64_t n, const int32_t* __restrict__ u0_vertex, const double* __restrict__ u0,
+                            double2* __restrict__ u) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * kMR; i += (int64_t)gridDim.x * blockDim.x)
+        u[i] = make_double2(u0 ? u0[u0_vertex[i / kMR]] : 1.0, 0.0);
+}
+
+__global__ void k_sbcm_extract(int64_t n, int lane, const double2* __restrict__ u, double2* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = u[i * kMR + lane];
+}
+
 // ------------------------------------------------------------------ host --
 static void map_status_sbc(int st) {
     switch (st) {
@@ -767,6 +1059,7 @@ static void map_status_sbc(int st) {
         case DEV_TIMEOUT: throw Error(BT_ERR_TIMEOUT, "strong periodic stepper: a grid-wide wait ran out");
         case DEV_NOT_CONVERGED:
             throw Error(BT_ERR_NOT_CONVERGED, "strong periodic stepper: BiCGSTAB reached max_iterations or broke down");
+        case DEV_BREAKDOWN: throw Error(BT_ERR_BREAKDOWN, "strong periodic stepper: BiCGSTAB breakdown");
         default: throw Error(BT_ERR_CUDA, "strong periodic stepper: device error");
     }
 }
@@ -783,6 +1076,137 @@ void set_strong(bt_ctx* ctx, const int32_t* dir) {
 }
 
 bool strong_active(const bt_ctx* ctx) { return ctx->strong && ctx->strong->on; }
+
+// One launch of the batched stepper for the signals grp (one gradient direction
+// and sequence, 2..32 signals); outputs go to the signals' places in the call.
+static float run_strong_multi(bt_ctx* ctx, Strong& P, const std::vector<int32_t>& grp, const double* q,
+                              const double* gdir, const int32_t* seq, const double* d_u0, double rtol, int32_t maxit,
+                              double* sig, double* comp_sig, bt_stats* st) {
+    Schedule& S = ctx->sched;
+    Mesh& m = ctx->mesh;
+    cudaStream_t s = ctx->stream;
+    const int64_t n = P.n, nnz = P.nnz;
+    const int R = (int)grp.size();
+    int per_sm = 0;
+    BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_sbc_multi, kThreadsS, 0));
+    BT_REQUIRE(per_sm >= 1, BT_ERR_CUDA, "strong periodic batched stepper does not fit on an SM");
+    const int64_t need = std::max<int64_t>(1, (n + kThreadsS / 32 - 1) / (kThreadsS / 32));   // a warp per row
+    P.mblocks = (int32_t)std::min<int64_t>((int64_t)per_sm * ctx->num_sms, need);
+    const size_t vn = (size_t)n * kMR;
+    for (auto* b : {&P.mu[0], &P.mu[1], &P.mu[2], &P.mr, &P.mrh, &P.mp, &P.mv, &P.ms, &P.mt, &P.my, &P.mz, &P.mdinv}) {
+        b->alloc(vn);
+        b->zero(s);
+    }
+    P.mpart.alloc((size_t)2 * P.mblocks * kMR * kMV);
+    P.mfin.alloc((size_t)kMR * kMV);
+    P.mout.alloc((size_t)kMR * 3);
+    P.mrel.alloc((size_t)kMR * S.n_steps);
+    P.iters.alloc(S.n_steps);
+    P.bar.alloc(4);
+    P.status.alloc(1);
+    // unit-q pack of the direction: are = M/k + theta S, md = theta (M_D)_g, ev = theta E_g
+    const double* g = gdir + 3 * grp.front();
+    const double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    P.are.alloc(nnz);
+    P.mdg.alloc(nnz);
+    P.eg.alloc(nnz);
+    const int pack_blocks = (int)std::min<int64_t>((nnz + 255) / 256, (int64_t)ctx->num_sms * 8);
+    k_sbc_pack<<<std::max(1, pack_blocks), 256, 0, s>>>(nnz, P.m, P.s, P.md6, P.e3, 1.0 / S.dt, S.theta, 1.0,
+                                                         g[0] / gn, g[1] / gn, g[2] / gn, P.are, P.mdg, P.eg);
+    BT_CUDA(cudaGetLastError());
+    std::vector<double> hq(kMR, 0.0), hFn((size_t)kMR * S.n_steps, 0.0), hFo((size_t)kMR * S.n_steps, 0.0);
+    const int32_t srow = seq ? seq[grp.front()] : 0;
+    BT_REQUIRE(srow >= 0 && srow < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
+    for (int l = 0; l < R; ++l) {
+        hq[l] = q[grp[l]];
+        for (int k = 0; k < S.n_steps; ++k) {
+            hFn[(size_t)l * S.n_steps + k] = S.F_new[(size_t)srow * S.n_steps + k];
+            hFo[(size_t)l * S.n_steps + k] = S.F_old[(size_t)srow * S.n_steps + k];
+        }
+    }
+    P.mq.upload(hq.data(), kMR, s);
+    P.mFn.upload(hFn.data(), hFn.size(), s);
+    P.mFo.upload(hFo.data(), hFo.size(), s);
+    const int init_blocks = (int)std::min<int64_t>((int64_t)((vn + 255) / 256), (int64_t)ctx->num_sms * 8);
+    k_sbcm_init<<<std::max(1, init_blocks), 256, 0, s>>>(n, P.u0_vertex, d_u0, P.mu[0]);
+    BT_CUDA(cudaGetLastError());
+    P.bar.zero(s);
+    P.status.zero(s);
+    SbcMultiArgs a{};
+    a.n = n;
+    a.row_ptr = P.row_ptr;
+    a.col = P.col;
+    a.diag = P.diag;
+    a.rcomp = P.rcomp;
+    a.m = P.m;
+    a.are = P.are;
+    a.md = P.mdg;
+    a.ev = P.eg;
+    a.w = P.w;
+    a.q = P.mq;
+    a.Fn = P.mFn;
+    a.Fo = P.mFo;
+    a.inv_k = 1.0 / S.dt;
+    a.R = R;
+    a.n_steps = S.n_steps;
+    a.maxit = maxit;
+    a.extrapolate = ctx->opt_fp64_extrapolate >= 1 ? 1 : 0;
+    a.rtol2 = rtol * rtol;
+    a.u0 = P.mu[0];
+    a.u1 = P.mu[1];
+    a.u2 = P.mu[2];
+    a.r = P.mr;
+    a.rh = P.mrh;
+    a.p = P.mp;
+    a.v = P.mv;
+    a.sv = P.ms;
+    a.t = P.mt;
+    a.y = P.my;
+    a.z = P.mz;
+    a.dinv = P.mdinv;
+    a.partials = P.mpart;
+    a.fin = P.mfin;
+    a.bar = P.bar;
+    a.status = P.status;
+    a.iters = P.iters;
+    a.relres = P.mrel;
+    a.out = P.mout;
+    a.wait_ns = ctx->opt_wait_ns;
+    void* args[] = {&a};
+    BT_CUDA(cudaEventRecord(ctx->ev1, s));
+    BT_CUDA(cudaLaunchCooperativeKernel((const void*)k_step_sbc_multi, dim3(P.mblocks), dim3(kThreadsS), args, 0, s));
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    int hst = 0;
+    std::vector<double> hout((size_t)kMR * 3), hrel((size_t)kMR * S.n_steps);
+    std::vector<int32_t> hit(S.n_steps);
+    P.status.download(&hst, 1, s);
+    P.mout.download(hout.data(), hout.size(), s);
+    P.mrel.download(hrel.data(), hrel.size(), s);
+    P.iters.download(hit.data(), S.n_steps, s);
+    BT_CUDA(cudaStreamSynchronize(s));
+    map_status_sbc(hst);
+    float ms = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
+    const unsigned eb = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8);
+    for (int l = 0; l < R; ++l) {
+        const int32_t sg = grp[l];
+        k_sbcm_extract<<<std::max(1u, eb), 256, 0, s>>>(n, l, P.mu[S.n_steps % 3], P.saved.p + (size_t)sg * n);
+        sig[sg] = hout[(size_t)l * 3];
+        if (comp_sig)
+            for (int c = 0; c < m.n_comp && c < 2; ++c) comp_sig[(size_t)sg * m.n_comp + c] = hout[(size_t)l * 3 + 1 + c];
+        for (int k = 0; k < S.n_steps; ++k) {
+            ctx->last_iters[(size_t)sg * S.n_steps + k] = hit[k];
+            if (st) {
+                st->max_iterations = std::max(st->max_iterations, hit[k]);
+                st->total_iterations += hit[k];
+                st->max_rel_residual = std::max(st->max_rel_residual, hrel[(size_t)l * S.n_steps + k]);
+            }
+        }
+    }
+    BT_CUDA(cudaGetLastError());
+    if (st) st->kernel_launches += 3 + R;
+    return ms;
+}
 
 void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, const int32_t* seq,
                   const double* u0, double rtol, int32_t maxit, double* sig, double* comp_sig, bt_stats* st) {
@@ -844,8 +1268,35 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
     std::vector<double> hFn(S.n_steps), hFo(S.n_steps), hres(S.n_steps), hout(kRedS);
     std::vector<int32_t> hit(S.n_steps);
     float stepper_ms = 0.0f;
+    // signals of one gradient direction and sequence go through the batched stepper
+    // in groups of up to 32; a signal alone takes the single-signal stepper
+    std::vector<std::vector<int32_t>> groups;
+    {
+        std::vector<int32_t> ord(nsig);
+        for (int32_t i = 0; i < nsig; ++i) ord[i] = i;
+        auto key = [&](int32_t i) {
+            const double* g = gdir + 3 * i;
+            const double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+            return std::make_tuple(seq ? seq[i] : 0, g[0] / gn, g[1] / gn, g[2] / gn);
+        };
+        std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return key(x) < key(y); });
+        for (int32_t i = 0; i < nsig; ++i) {
+            if (ctx->opt_strong_batch && !groups.empty() && key(groups.back().front()) == key(ord[i]) &&
+                (int)groups.back().size() < kMR)
+                groups.back().push_back(ord[i]);
+            else
+                groups.push_back({ord[i]});
+        }
+    }
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
-    for (int32_t sg = 0; sg < nsig; ++sg) {
+    // (a batched launch costs about what one single-signal launch does on small
+    // systems, so it pays from three signals of a direction on)
+    for (const auto& grp : groups) {
+      if (grp.size() >= 3) {
+        stepper_ms += run_strong_multi(ctx, P, grp, q, gdir, seq, u0 ? d_u0.p : nullptr, rtol, maxit, sig, comp_sig, st);
+        continue;
+      }
+      for (const int32_t sg : grp) {
         const int32_t row = seq ? seq[sg] : 0;
         BT_REQUIRE(row >= 0 && row < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
         for (int k = 0; k < S.n_steps; ++k) {
@@ -932,6 +1383,7 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
             }
         }
         if (st) st->kernel_launches += 3;
+      }
     }
     BT_CUDA(cudaEventRecord(ctx->ev2, s));
     BT_CUDA(cudaEventSynchronize(ctx->ev2));
