@@ -46,7 +46,6 @@
 #include <array>
 #include <cmath>
 #include <map>
-#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -78,7 +77,7 @@ struct Strong {
     // batched stepper (several signals of one gradient direction): vectors [row][32]
     int32_t mblocks = 0;
     DevBuf<double2> mu[3], mr, mrh, mp, mv, ms, mt, my, mz, mdinv;
-    DevBuf<double> mq, mFn, mFo, mpart, mfin, mout, mrel;
+    DevBuf<double> mq, mg, mFn, mFo, mpart, mfin, mout, mrel;
 };
 
 namespace {
@@ -766,10 +765,11 @@ __global__ void __launch_bounds__(kThreadsS, 2) k_step_sbc(SbcArgs a) {
 }
 
 // ----------------------------------------------------- batched stepper --
-// Up to 32 signals of one gradient direction in one cooperative launch: a warp
-// takes a row, its lane l the row's value of signal l, so each stored entry
-// (column, A_re, M_D, E of the unit-q pack) is read once for all of them and a
-// signal's coefficients q^2 F^2 and q F multiply per lane.  Every signal runs its
+// Up to 32 signals of one sequence in one cooperative launch: a warp takes a
+// row, its lane l the row's value of signal l, so each stored entry (column,
+// M/k + theta S, the six M_D and three E components) is read once for all of
+// them; lane l forms its signal's (M_D)_g and E_g from its own direction and
+// scales them by theta q^2 F^2 and theta q F.  Every signal runs its
 // own Jacobi-BiCGSTAB (its own rho, alpha, omega; a converged signal stops
 // moving) and the launch iterates until all have converged.  Sums over rows go
 // per signal through two-stage grid reductions (block partials; one warp per
@@ -785,10 +785,14 @@ struct SbcMultiArgs {
     const int32_t* __restrict__ rcomp;
     const double* __restrict__ m;
     const double* __restrict__ are;
-    const double* __restrict__ md;   // theta (M_D)_g of unit q
-    const double* __restrict__ ev;   // theta E_g of unit q
+    const double* __restrict__ md6;  // six M_D components per entry (xx, yy, zz, 2xy, 2xz, 2yz)
+    const double* __restrict__ e3;   // three E components per entry (g_x, g_y, g_z)
+    const double* __restrict__ md;   // one direction for all lanes (nullable): theta (M_D)_g per entry
+    const double* __restrict__ ev;   //   and theta E_g per entry
     const double* __restrict__ w;
     const double* __restrict__ q;    // [kMR]
+    const double* __restrict__ gl;   // [kMR][3] unit gradient direction per signal
+    double theta;
     const double* __restrict__ Fn;   // [kMR][n_steps]
     const double* __restrict__ Fo;
     double inv_k;
@@ -846,6 +850,22 @@ __global__ void __launch_bounds__(kThreadsS, 1) k_step_sbc_multi(SbcMultiArgs a)
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const double ql = live ? a.q[lane] : 0.0;
+    const double gx = live ? a.gl[lane * 3] : 0.0, gy = live ? a.gl[lane * 3 + 1] : 0.0,
+                 gz = live ? a.gl[lane * 3 + 2] : 0.0;
+    const double gg[6] = {gx * gx, gy * gy, gz * gz, gx * gy, gx * gz, gy * gz};
+    // this signal's theta (M_D)_g and theta E_g of stored entry e
+    // (a group of one direction reads them precombined)
+    const bool shared = a.md != nullptr;
+    auto mdg = [&](int32_t e) {
+        if (shared) return a.md[e];
+        const double* d = a.md6 + (size_t)6 * e;
+        return a.theta * (d[0] * gg[0] + d[1] * gg[1] + d[2] * gg[2] + d[3] * gg[3] + d[4] * gg[4] + d[5] * gg[5]);
+    };
+    auto eg = [&](int32_t e) {
+        if (shared) return a.ev[e];
+        const double* d = a.e3 + (size_t)3 * e;
+        return a.theta * (d[0] * gx + d[1] * gy + d[2] * gz);
+    };
     double2* U[3] = {a.u0, a.u1, a.u2};
     int its_total = 0;
     (void)its_total;
@@ -866,7 +886,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) k_step_sbc_multi(SbcMultiArgs a)
             const int32_t e0 = a.row_ptr[row], e1 = a.row_ptr[row + 1];
             for (int32_t e = e0; e < e1; ++e) {
                 const size_t cj = (size_t)a.col[e] * kMR + lane;
-                const double ar = a.are[e], mdv = a.md[e], mm = a.m[e], evv = a.ev[e];
+                const double ar = a.are[e], mdv = mdg(e), mm = a.m[e], evv = eg(e);
                 const double2 xv = un[cj];
                 double2 x0 = xv;
                 if (ext) {
@@ -882,7 +902,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) k_step_sbc_multi(SbcMultiArgs a)
             }
             const int32_t d = a.diag[row];
             const double2 ri = make_double2(b.x - ax.x, b.y - ax.y);
-            a.dinv[vi] = cinv(make_double2(a.are[d] + c2 * a.md[d], c1 * a.ev[d]));
+            a.dinv[vi] = cinv(make_double2(a.are[d] + c2 * mdg(d), c1 * eg(d)));
             a.r[vi] = ri;
             a.rh[vi] = ri;
             a.p[vi] = make_double2(0.0, 0.0);
@@ -936,7 +956,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) k_step_sbc_multi(SbcMultiArgs a)
                     const size_t vi = (size_t)row * kMR + lane;
                     double2 acc = make_double2(0.0, 0.0);
                     for (int32_t e = a.row_ptr[row]; e < a.row_ptr[row + 1]; ++e) {
-                        const double ra = a.are[e] + c2 * a.md[e], ia = c1 * a.ev[e];
+                        const double ra = a.are[e] + c2 * mdg(e), ia = c1 * eg(e);
                         const double2 xv = a.y[(size_t)a.col[e] * kMR + lane];
                         acc.x += ra * xv.x - ia * xv.y;
                         acc.y += ra * xv.y + ia * xv.x;
@@ -970,7 +990,7 @@ __global__ void __launch_bounds__(kThreadsS, 1) k_step_sbc_multi(SbcMultiArgs a)
                     const size_t vi = (size_t)row * kMR + lane;
                     double2 acc = make_double2(0.0, 0.0);
                     for (int32_t e = a.row_ptr[row]; e < a.row_ptr[row + 1]; ++e) {
-                        const double ra = a.are[e] + c2 * a.md[e], ia = c1 * a.ev[e];
+                        const double ra = a.are[e] + c2 * mdg(e), ia = c1 * eg(e);
                         const double2 xv = a.z[(size_t)a.col[e] * kMR + lane];
                         acc.x += ra * xv.x - ia * xv.y;
                         acc.y += ra * xv.y + ia * xv.x;
@@ -1077,8 +1097,8 @@ void set_strong(bt_ctx* ctx, const int32_t* dir) {
 
 bool strong_active(const bt_ctx* ctx) { return ctx->strong && ctx->strong->on; }
 
-// One launch of the batched stepper for the signals grp (one gradient direction
-// and sequence, 2..32 signals); outputs go to the signals' places in the call.
+// One launch of the batched stepper for the signals grp (one sequence, 3..32
+// signals, any directions); outputs go to the signals' places in the call.
 static float run_strong_multi(bt_ctx* ctx, Strong& P, const std::vector<int32_t>& grp, const double* q,
                               const double* gdir, const int32_t* seq, const double* d_u0, double rtol, int32_t maxit,
                               double* sig, double* comp_sig, bt_stats* st) {
@@ -1104,27 +1124,39 @@ static float run_strong_multi(bt_ctx* ctx, Strong& P, const std::vector<int32_t>
     P.iters.alloc(S.n_steps);
     P.bar.alloc(4);
     P.status.alloc(1);
-    // unit-q pack of the direction: are = M/k + theta S, md = theta (M_D)_g, ev = theta E_g
-    const double* g = gdir + 3 * grp.front();
-    const double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    // are = M/k + theta S; when every signal of the group has one direction, also
+    // that direction's theta (M_D)_g and theta E_g (unit q), else each lane forms its own
+    bool one_dir = true;
+    const double* g0 = gdir + 3 * grp.front();
+    const double g0n = std::sqrt(g0[0] * g0[0] + g0[1] * g0[1] + g0[2] * g0[2]);
+    for (int l = 1; l < R; ++l) {
+        const double* g = gdir + 3 * grp[l];
+        const double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        for (int k = 0; k < 3; ++k) one_dir = one_dir && g[k] / gn == g0[k] / g0n;
+    }
     P.are.alloc(nnz);
     P.mdg.alloc(nnz);
     P.eg.alloc(nnz);
     const int pack_blocks = (int)std::min<int64_t>((nnz + 255) / 256, (int64_t)ctx->num_sms * 8);
     k_sbc_pack<<<std::max(1, pack_blocks), 256, 0, s>>>(nnz, P.m, P.s, P.md6, P.e3, 1.0 / S.dt, S.theta, 1.0,
-                                                         g[0] / gn, g[1] / gn, g[2] / gn, P.are, P.mdg, P.eg);
+                                                         g0[0] / g0n, g0[1] / g0n, g0[2] / g0n, P.are, P.mdg, P.eg);
     BT_CUDA(cudaGetLastError());
-    std::vector<double> hq(kMR, 0.0), hFn((size_t)kMR * S.n_steps, 0.0), hFo((size_t)kMR * S.n_steps, 0.0);
+    std::vector<double> hq(kMR, 0.0), hg((size_t)kMR * 3, 0.0), hFn((size_t)kMR * S.n_steps, 0.0),
+        hFo((size_t)kMR * S.n_steps, 0.0);
     const int32_t srow = seq ? seq[grp.front()] : 0;
     BT_REQUIRE(srow >= 0 && srow < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
     for (int l = 0; l < R; ++l) {
         hq[l] = q[grp[l]];
+        const double* g = gdir + 3 * grp[l];
+        const double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        for (int k = 0; k < 3; ++k) hg[(size_t)l * 3 + k] = g[k] / gn;
         for (int k = 0; k < S.n_steps; ++k) {
             hFn[(size_t)l * S.n_steps + k] = S.F_new[(size_t)srow * S.n_steps + k];
             hFo[(size_t)l * S.n_steps + k] = S.F_old[(size_t)srow * S.n_steps + k];
         }
     }
     P.mq.upload(hq.data(), kMR, s);
+    P.mg.upload(hg.data(), hg.size(), s);
     P.mFn.upload(hFn.data(), hFn.size(), s);
     P.mFo.upload(hFo.data(), hFo.size(), s);
     const int init_blocks = (int)std::min<int64_t>((int64_t)((vn + 255) / 256), (int64_t)ctx->num_sms * 8);
@@ -1140,8 +1172,12 @@ static float run_strong_multi(bt_ctx* ctx, Strong& P, const std::vector<int32_t>
     a.rcomp = P.rcomp;
     a.m = P.m;
     a.are = P.are;
-    a.md = P.mdg;
-    a.ev = P.eg;
+    a.md6 = P.md6;
+    a.e3 = P.e3;
+    a.md = one_dir ? P.mdg.p : nullptr;
+    a.ev = one_dir ? P.eg.p : nullptr;
+    a.gl = P.mg;
+    a.theta = S.theta;
     a.w = P.w;
     a.q = P.mq;
     a.Fn = P.mFn;
@@ -1268,18 +1304,24 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
     std::vector<double> hFn(S.n_steps), hFo(S.n_steps), hres(S.n_steps), hout(kRedS);
     std::vector<int32_t> hit(S.n_steps);
     float stepper_ms = 0.0f;
-    // signals of one gradient direction and sequence go through the batched stepper
-    // in groups of up to 32; a signal alone takes the single-signal stepper
+    // signals of one sequence go through the batched stepper in groups of up to 32
+    // (any directions); a group of one or two takes the single-signal stepper
     std::vector<std::vector<int32_t>> groups;
     {
         std::vector<int32_t> ord(nsig);
         for (int32_t i = 0; i < nsig; ++i) ord[i] = i;
-        auto key = [&](int32_t i) {
+        auto key = [&](int32_t i) { return seq ? seq[i] : 0; };
+        // by sequence, then direction: a b-series of one direction fills a launch
+        // that reads its direction terms precombined
+        auto dir = [&](int32_t i) {
             const double* g = gdir + 3 * i;
             const double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-            return std::make_tuple(seq ? seq[i] : 0, g[0] / gn, g[1] / gn, g[2] / gn);
+            return std::array<double, 3>{g[0] / gn, g[1] / gn, g[2] / gn};
         };
-        std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return key(x) < key(y); });
+        std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) {
+            if (key(x) != key(y)) return key(x) < key(y);
+            return dir(x) < dir(y);
+        });
         for (int32_t i = 0; i < nsig; ++i) {
             if (ctx->opt_strong_batch && !groups.empty() && key(groups.back().front()) == key(ord[i]) &&
                 (int)groups.back().size() < kMR)
@@ -1290,7 +1332,7 @@ void solve_strong(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir
     }
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
     // (a batched launch costs about what one single-signal launch does on small
-    // systems, so it pays from three signals of a direction on)
+    // systems, so it pays from three signals on)
     for (const auto& grp : groups) {
       if (grp.size() >= 3) {
         stepper_ms += run_strong_multi(ctx, P, grp, q, gdir, seq, u0 ? d_u0.p : nullptr, rtol, maxit, sig, comp_sig, st);

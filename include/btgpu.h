@@ -377,9 +377,9 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *   "mixed.sort_signals"    1 (default): bt_solve's mixed path orders the signals by (sequence, |q|)
  *                           before cutting them into launches of 256 and warps of 32, so signals of
  *                           similar convergence share them (outputs keep the call's order); 0: as given
- *   "strong.batch"          1 (default): in the strong pseudo-periodic form, signals of one gradient
- *                           direction and sequence share a batched launch (up to 32, one lane each);
- *                           0: one launch per signal
+ *   "strong.batch"          1 (default): in the strong pseudo-periodic form, signals of one sequence
+ *                           share batched launches (up to 32, one lane each, any directions; groups of
+ *                           one or two run alone); 0: one launch per signal
  *   "fp64.extrapolate"      order of the FP64 path's initial guess, extrapolated in time from the
  *                           last states: 4 (default), 3, 2, 1 (2 u_n - u_{n-1}) or 0 (u_n); the strong
  *                           pseudo-periodic stepper uses 2 u_n - u_{n-1} for any order >= 1

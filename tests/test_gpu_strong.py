@@ -232,9 +232,9 @@ def test_anisotropic_tensor_t2_field_and_initial_condition(pkg, lib):
 
 
 def test_batched_stepper_matches_single(pkg, lib):
-    """Signals of one direction share the batched strong stepper (one lane each);
-    the same signals one launch each give the same values (1e-10), mixed
-    directions and sequences are grouped, and outputs keep the call's order."""
+    """Signals share the batched strong stepper (one lane each, its own direction);
+    the same signals one launch each give the same values (1e-10), and outputs
+    keep the call's order."""
     xyz, tets = pkg.meshgen.kuhn_box(-5.0, 5.0, 6)
     reg = cube_cylinder_regions(xyz, tets, 2.6)
     seq = pkg.sequences.pgse(DELTA, BIGDELTA)
@@ -242,18 +242,29 @@ def test_batched_stepper_matches_single(pkg, lib):
     ctx = strong_ctx(pkg, xyz, tets, reg, 2, [3e-3, 1.5e-3], [0.0, 1.0 / 6e4], kp, [1, 1, 1], seq)
     bs = [500.0, 1000.0, 1500.0, 2000.0, 2500.0, 3000.0]
     g1, g2 = np.array([1.0, 0.4, 0.3]), np.array([0.2, 0.5, 1.0])
-    q = np.array([pkg.sequences.b_to_q(b, seq.int4gb()) for b in bs] * 2)
-    g = np.array([g1] * 6 + [g2] * 6)
-    perm = np.random.default_rng(2).permutation(12)            # interleave the two groups in the call
+    q = np.array([pkg.sequences.b_to_q(b, seq.int4gb()) for b in bs] * 2
+                 + [pkg.sequences.b_to_q(2200.0, seq.int4gb())] * 30)
+    rng = np.random.default_rng(2)
+    g3 = rng.normal(size=(30, 3))                                # 30 more directions: 42 signals, two launches
+    g = np.concatenate([np.array([g1] * 6 + [g2] * 6), g3 / np.linalg.norm(g3, axis=1)[:, None]])
+    perm = rng.permutation(42)                                   # interleaved in the call
     q, g = q[perm], g[perm]
     ctx.set_option("strong.batch", 1)
     a = ctx.solve(q, g, rtol=1e-13, max_iterations=5000, compartments=True)
-    ua = [ctx.solution(i) for i in (0, 5, 11)]
+    ua = [ctx.solution(i) for i in (0, 5, 41)]
     ctx.set_option("strong.batch", 0)
     b = ctx.solve(q, g, rtol=1e-13, max_iterations=5000, compartments=True)
     assert np.max(np.abs(a["signal"] - b["signal"]) / np.abs(b["signal"])) <= 1e-10
     assert np.allclose(a["compartments"], b["compartments"], rtol=1e-10, atol=1e-12)
-    for i, u in zip((0, 5, 11), ua):
+    for i, u in zip((0, 5, 41), ua):
         ub = ctx.solution(i)
         assert np.max(np.abs(u - ub)) <= 1e-10 * np.max(np.abs(ub))
+    # a b-series of one direction (the launch reads its direction terms precombined)
+    qs = np.array([pkg.sequences.b_to_q(b, seq.int4gb()) for b in np.linspace(500.0, 4000.0, 8)])
+    gs = np.tile(g2 / np.linalg.norm(g2), (8, 1))
+    ctx.set_option("strong.batch", 1)
+    a = ctx.solve(qs, gs, rtol=1e-13, max_iterations=5000)
+    ctx.set_option("strong.batch", 0)
+    b = ctx.solve(qs, gs, rtol=1e-13, max_iterations=5000)
+    assert np.max(np.abs(a["signal"] - b["signal"]) / np.abs(b["signal"])) <= 1e-10
     ctx.close()
