@@ -254,6 +254,26 @@ def duplicated_strong(xyz, tets, region, D, invT2, kappa_pair, pdir, g, field=No
     vals = (icoef[:, None, None] * imass).reshape(-1, 9)
     E = E - _coo(np.repeat(d0, 3, axis=1), np.tile(d0, 3), vals, n) \
           + _coo(np.repeat(d1, 3, axis=1), np.tile(d1, 3), vals, n)
+    # the reference's outer term is phase-blind: on an exterior facet of a c-cell it
+    # also acts on the other compartment's rows at the facet's interface vertices.
+    # Summed over the folded space it must vanish (it does between matching periodic
+    # faces) for a per-compartment system to equal the reference; the engine refuses
+    # a gradient along which it does not (the same rule here)
+    excess = {}
+    dscale = np.max(np.abs(ecoef)) * np.max(emass) if len(ecoef) else 0.0
+    for f in range(len(ec)):
+        cf = field[ec[f]]
+        for i in range(3):
+            vi = ev[f, i]
+            for oc in range(nf):
+                if oc == cf or not touch[vi, oc]:
+                    continue
+                for j in range(3):
+                    key = (cls[vi], oc, cls[ev[f, j]])
+                    excess[key] = excess.get(key, 0.0) + ecoef[f] * emass[f, i, j]
+    if any(abs(v) > 1e-10 * dscale for v in excess.values()):
+        raise ValueError("(D g).n does not vanish where the phase-blind outer term reaches live rows "
+                         "(the reference's literal form differs from any per-compartment system there)")
     w = np.zeros(n)
     np.add.at(w, cd.ravel(), np.repeat(vol / 4.0, 4))
     dof_class, dof_field = np.nonzero(live)

@@ -120,16 +120,17 @@ def test_literal_equals_duplicated_two_compartments(pdir, g):
 def test_literal_differs_when_a_non_periodic_face_sees_the_gradient():
     """With g.n != 0 on a non-periodic face the literal form couples the dead
     rows of the other compartment there (its outer term is not phase
-    weighted): the two restatements then differ, which is why the engine
-    requires that face term to vanish."""
+    weighted): no per-compartment system equals it, and the duplicated system
+    refuses that gradient, as the engine does."""
     xyz, tets, reg = _box_with_cylinder()
-    q = oracle.bvalue_to_q(2500, SEQ.int4gb())
     g = (0.3, 0.2, 1.0)
-    sd = strong.duplicated_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 0], g)
+    with pytest.raises(ValueError, match="phase-blind"):
+        strong.duplicated_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 0], g)
     sl = strong.literal_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 0], g)
-    a = strong.solve_strong(sd, SEQ, q, 100.0)
-    b = strong.solve_literal_strong(sl, SEQ, q, 100.0)
-    assert abs(a["normalized"] - b["normalized"]) > 1e-9
+    dead = np.nonzero(sl["dead"])[0]
+    live = np.nonzero(~sl["dead"])[0]
+    # the literal form's first-order block couples live rows to dead columns
+    assert np.abs(sl["Q1"][live][:, dead]).max() > 0.0
 
 
 def test_non_periodic_compartments_are_rejected():
@@ -160,3 +161,44 @@ def test_operator_structure():
     E = sd["E"].toarray()
     assert np.abs(E + E.T).max() > 1e-6 * np.abs(E).max()
     assert np.abs(E - E.T).max() > 1e-6 * np.abs(E).max()
+
+
+def test_literal_equals_duplicated_with_a_tensor_field():
+    """Per-cell anisotropic tensor (symmetric, varying per cube column so it is
+    periodic across the z faces) and per-cell 1/T2: both restatements agree."""
+    xyz, tets, reg = _box_with_cylinder(n=6)
+    X = xyz[tets].min(axis=1)
+    col = (np.rint((X[:, 0] + 5.0) / (10.0 / 6)) * 6 + np.rint((X[:, 1] + 5.0) / (10.0 / 6))).astype(int)
+    rng = np.random.default_rng(4)
+    base = np.where(reg == 1, 1.5e-3, 3e-3)
+    A = rng.normal(size=(36, 3, 3)) * 0.2
+    Dt = base[:, None, None] * (np.eye(3)[None] + 0.25 * (A[col] + np.transpose(A[col], (0, 2, 1))))
+    iT2 = (1.0 / (5e4 + 5e4 * rng.random(36)))[col]
+    q = oracle.bvalue_to_q(2000, SEQ.int4gb())
+    g = (0.5, 0.7, 0.3)
+    sd = strong.duplicated_strong(xyz, tets, reg, Dt, iT2, 2e-5, [1, 1, 1], g)
+    sl = strong.literal_strong(xyz, tets, reg, Dt, iT2, 2e-5, [1, 1, 1], g)
+    a = strong.solve_strong(sd, SEQ, q, 100.0)
+    b = strong.solve_literal_strong(sl, SEQ, q, 100.0)
+    assert abs(a["normalized"] - b["normalized"]) < 1e-12
+    assert np.allclose(a["compartments"], b["compartments"], rtol=1e-11, atol=1e-12)
+
+
+def test_phase_blind_term_reaching_live_rows_is_refused():
+    """On the 5-cube box the cylinder's interface vertices on the z faces share
+    exterior facets with edge vertices the reference's map leaves unpaired
+    ((x, ymin, z) columns are masters), so the phase-blind outer term does not
+    cancel between the z faces: the literal form differs from the per-compartment
+    system along g_z, which refuses it (as the engine does); g in the x-y plane is
+    exact."""
+    xyz, tets, reg = _box_with_cylinder(n=5)
+    q = oracle.bvalue_to_q(2000, SEQ.int4gb())
+    with pytest.raises(ValueError, match="phase-blind"):
+        strong.duplicated_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 1], (0.5, 0.7, 0.3))
+    sl = strong.literal_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 1], (0.5, 0.7, 0.3))
+    sd0 = strong.duplicated_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 1], (0.5, 0.7, 0.0))
+    sl0 = strong.literal_strong(xyz, tets, reg, 3e-3, 0.0, 2e-5, [1, 1, 1], (0.5, 0.7, 0.0))
+    a = strong.solve_strong(sd0, SEQ, q, 100.0, max_steps=20)
+    b = strong.solve_literal_strong(sl0, SEQ, q, 100.0, max_steps=20)
+    assert abs(a["normalized"] - b["normalized"]) < 1e-12
+    assert sl["N"] > 0
