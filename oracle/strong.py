@@ -35,9 +35,11 @@ In complex form, per compartment c with outward normal n_c on its boundary::
 compartment) pair; ``literal_strong`` assembles the reference's real mixed
 space with the phase weighting and ``ident_zeros``.  The two agree when the
 compartments are periodic (a folded vertex touches the same compartments as
-its master; ``duplicated_strong`` raises otherwise) and every exterior facet
-off the periodic faces has ``(D g).n = 0``: the literal form's phase-blind
-outer term then cancels between opposite faces and its dead rows decouple.
+its master) and the literal form's phase-blind outer term, summed over the
+folded space, does not reach live rows of the other compartment (it cancels
+between matching periodic faces and vanishes where ``(D g).n = 0``; it does
+not cancel next to the edge columns the reference's map leaves unpaired);
+``duplicated_strong`` raises in the other cases, as the engine does.
 ``tests/test_oracle_strong.py`` checks that and pins the homogeneous box
 against the closed-form product of the uniform solution.
 
