@@ -867,8 +867,6 @@ __global__ void __launch_bounds__(kThreadsS, 1) k_step_sbc_multi(SbcMultiArgs a)
         return a.theta * (d[0] * gx + d[1] * gy + d[2] * gz);
     };
     double2* U[3] = {a.u0, a.u1, a.u2};
-    int its_total = 0;
-    (void)its_total;
     for (int32_t step = 0; step < a.n_steps; ++step) {
         const double F = live ? a.Fn[(size_t)lane * a.n_steps + step] : 0.0;
         const double Fp = live ? a.Fo[(size_t)lane * a.n_steps + step] : 0.0;
