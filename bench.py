@@ -87,6 +87,20 @@ def alg_bytes_fp64(n, nnz, steps, iters):
     return steps * per_step + iters * per_iter
 
 
+def alg_bytes_fp64_pair(n, nnz, its):
+    """Minimum unique bytes of one k_step64_pair launch (two signals of one
+    direction; its[j][k] = COCG iterations of signal j at step k).
+
+    The matrix (column, A_re, J_g: nnz*20 + 4n) is read once per pair iteration,
+    max(its[0][k], its[1][k]) of them at step k; the vector traffic (160n) is per
+    signal and iteration.  Per step: the right-hand-side matrix once
+    (nnz*28 + 4n) and 32n of vectors per signal.
+    """
+    its = np.asarray(its, np.int64)
+    per_step = (nnz * 28 + 4 * n) * its.shape[1] + 2 * 32 * n * its.shape[1]
+    return per_step + (nnz * 20 + 4 * n) * int(its.max(axis=0).sum()) + 160 * n * int(its.sum())
+
+
 def alg_bytes_mixed(n, nnz, nsig, steps, iters, sweeps):
     """Minimum unique bytes of one k_batched launch of `nsig` signals.
 
@@ -273,22 +287,32 @@ def _context(pkg, w, local, stream):
 NOMINAL_HBM_GBS = 7900.0   # GB300 HBM3e nominal, for reference beside the measured copy bandwidth
 
 
-def roofline_fp64(info, st, n_sig, peak, peak_src, traffic):
-    iters = st["total_iterations"] / n_sig
-    byts = alg_bytes_fp64(info["n_dofs"], info["nnz"], st["steps"], iters)
-    launch_ms = st["stepper_ms"] / n_sig
+def roofline_fp64(info, st, its, peak, peak_src, traffic):
+    """Roofline of the headline's stepper launches.  its[j][k]: iterations of
+    signal j at step k.  Two signals of one direction share a k_step64_pair
+    launch (5 kernel launches per pair, 3 per single signal)."""
+    n_sig = len(its)
+    paired = n_sig == 2 and st["kernel_launches"] == 5
+    if paired:
+        byts = alg_bytes_fp64_pair(info["n_dofs"], info["nnz"], its)
+        launch_ms = st["stepper_ms"]
+        kernel = "k_step64_pair (persistent FP64 CN/COCG stepper, the two signals of one direction in one launch)"
+    else:
+        byts = alg_bytes_fp64(info["n_dofs"], info["nnz"], st["steps"], st["total_iterations"] / n_sig)
+        launch_ms = st["stepper_ms"] / n_sig
+        kernel = "k_step64 (persistent FP64 CN/COCG stepper, one launch per signal)"
     ach = byts / (launch_ms / 1e3) / 1e9
     out = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
            "traffic": traffic.get("bytes_per_launch") if traffic else None,
-           "kernel": "k_step64 (persistent FP64 CN/COCG stepper, one launch per signal)",
-           "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src,
+           "kernel": kernel, "bytes_per_launch": byts, "launch_ms": launch_ms, "peak_source": peak_src,
            "frac_of_nominal_7900": ach / NOMINAL_HBM_GBS}
     if traffic:
-        out["note"] = ("L2-resident: ncu counts %.0f MB of DRAM traffic per launch, %.3f%% of the %.0f GB of "
-                       "algorithmic bytes, so `achieved` counts L2-served bytes and `frac` is not an HBM "
-                       "fraction; the kernel is bound by the FP64 pipe (GB300 runs FP64 at a small fraction of "
-                       "FP32; ncu: FP64 pipe active 59%% of peak, profiles/k_step64_cfg2.md)"
-                       % (traffic["bytes_per_launch"] / 1e6, 100.0 * traffic["bytes_per_launch"] / byts, byts / 1e9))
+        out["note"] = ("L2-resident: ncu counts %.0f MB of DRAM traffic per launch of %s, %.3f%% of the %.0f GB "
+                       "of algorithmic bytes, so `achieved` counts L2-served bytes and `frac` is not an HBM "
+                       "fraction; the stepper is bound by the FP64 pipe (GB300 runs FP64 at a small fraction of "
+                       "FP32; profiles/k_step64_cfg2.md)"
+                       % (traffic["bytes_per_launch"] / 1e6, traffic.get("kernel", "the stepper"),
+                          100.0 * traffic["bytes_per_launch"] / byts, byts / 1e9))
     else:
         out["note"] = "no DRAM capture for this workload"
     return out
@@ -353,8 +377,9 @@ def gpu_run(args):
     value = len(job) * args.steps / (total_ms / 1e3)
     st = outs[-1]["stats"]
     norm = outs[-1]["signal"] / outs[-1]["S0"]
+    its = ctx.iterations(n_sig, st["steps"])
     gathered = replicas.gather_signals(mine, norm, len(job), device="cuda")
-    roof = roofline_fp64(info, st, n_sig, peak, peak_src, traffic.get("cfg2:fp64"))
+    roof = roofline_fp64(info, st, its, peak, peak_src, traffic.get("cfg2:fp64"))
     gold = golden_cfg2()
     err_oracle = [abs(float(v) - gold[b]) / abs(gold[b]) for (b, _, _), v in zip(sel, norm)
                   if tuple(dirs[0]) == (0.0, 1.0, 0.0) and b in gold] if rank == 0 else []

@@ -754,6 +754,12 @@ int bt_set_option(bt_ctx* ctx, const char* key, double value) {
         } else if (k == "fp64.extrapolate") {
             BT_REQUIRE(iv >= 0 && iv <= 4, BT_ERR_INVALID, "fp64.extrapolate must be in [0, 4]");
             ctx->opt_fp64_extrapolate = iv;
+        } else if (k == "fp64.pair_signals") {
+            BT_REQUIRE(iv >= 0 && iv <= 2, BT_ERR_INVALID, "fp64.pair_signals must be 0, 1 or 2");
+            ctx->opt_fp64_pair = iv;
+        } else if (k == "fp64.blocks_per_sm") {
+            BT_REQUIRE(iv >= -1 && iv <= 8, BT_ERR_INVALID, "fp64.blocks_per_sm must be in [-1, 8]");
+            ctx->opt_fp64_blocks_per_sm = iv;
         } else if (k == "wait.limit_ns") {
             BT_REQUIRE(value >= 1e4 && value <= 6e10, BT_ERR_INVALID, "wait.limit_ns must be in [1e4, 6e10]");
             ctx->opt_wait_ns = (unsigned long long)value;

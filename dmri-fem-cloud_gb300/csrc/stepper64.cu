@@ -64,6 +64,12 @@ struct Solver64 {
     DevBuf<double> gq;           // gradient direction for the pack kernel
     DevBuf<double2> saved;       // final solutions [nsig][n_pad]
     int32_t saved_nsig = 0;
+    // two signals a launch (k_step64_pair): [row][2] vectors, per-signal schedules and results
+    DevBuf<double2> pu[3], pr, pz, pp, pq, pdinv, ppa, ppj, phd;
+    DevBuf<double> pcn, pco, prelres, pout, ppartials;
+    DevBuf<int32_t> piters;
+    int32_t pair_blocks = 0;
+    int32_t pair_variant = 0;
 };
 
 struct StepArgs {
@@ -404,6 +410,356 @@ __global__ void __launch_bounds__(kThreads64) k_step64(StepArgs a) {
     if (blockIdx.x == 0 && threadIdx.x < kRed) a.out[threadIdx.x] = red[threadIdx.x];
 }
 
+// ------------------------------------------------------ two signals a launch --
+// Two signals of one gradient direction share A_re and J_g (only cn, co differ),
+// so one launch can step both: a thread loads a row's column indices and matrix
+// values once for the pair, its neighbour gathers fetch both signals' values from
+// one 32-byte pair slot ([row][signal] interleaved vectors), and the pair's grid
+// reductions share one set of barriers.  Each signal keeps its own COCG scalars
+// and stopping test; a converged signal's vectors stay untouched (uniform branch,
+// the sums are grid-identical) while the other one iterates.  The per-row
+// arithmetic of a signal is that of k_step64 in the same order.
+struct PairArgs {
+    int32_t n_slices;
+    const int32_t* __restrict__ sl_ptr;
+    const int32_t* __restrict__ sl_w;
+    const int32_t* __restrict__ col;
+    const double2* __restrict__ aj;
+    const double* __restrict__ bre;
+    const double* __restrict__ dA;
+    const double* __restrict__ dJ;
+    const double* __restrict__ w;
+    const int32_t* __restrict__ rcomp;
+    double2* u0;                         // vectors: [row][2], length 2 n_pad
+    double2* u1;
+    double2* u2;
+    double2* r;
+    double2* z;
+    double2* p;
+    double2* q;
+    double2* dinv;
+    double2* pa;
+    double2* pj;
+    double2* hd;                         // [4][3][2 n_pad]
+    double* partials;
+    unsigned* bar;
+    int* status;
+    const double* __restrict__ cn;       // [2][n_steps]
+    const double* __restrict__ co;       // [2][n_steps]
+    int32_t n_steps;
+    int32_t maxit;
+    int32_t extrapolate;
+    double rtol2;
+    int64_t n_pad;
+    int32_t* iters;                      // [2][n_steps]
+    double* relres;                      // [2][n_steps]
+    double* out;                         // [2][kRed]
+    unsigned long long wait_ns;
+    int32_t stall;
+};
+
+// w = A z for one row of the signals J0 .. J0 + NJ - 1 of the pair (sA = A_re z,
+// sJ = J_g z), four neighbour rows in flight as in k_step64's phase A.
+template <int J0, int NJ>
+__device__ __forceinline__ void pair_row_spmv(const int32_t* __restrict__ col, const double2* __restrict__ aj,
+                                              const double2* z, int32_t base, int32_t wdt, int lane,
+                                              double2 (&sA)[2], double2 (&sJ)[2]) {
+    int k = 0;
+    for (; k + 4 <= wdt; k += 4) {
+        int32_t cc[4];
+        double2 mm[4], zz[4][NJ];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int32_t e = base + (k + u) * 32 + lane;
+            cc[u] = col[e];
+            mm[u] = aj[e];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) zz[u][j] = z[2 * (size_t)cc[u] + J0 + j];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) {
+                double2& A = sA[J0 + j];
+                double2& J = sJ[J0 + j];
+                A.x = fma(mm[u].x, zz[u][j].x, A.x); A.y = fma(mm[u].x, zz[u][j].y, A.y);
+                J.x = fma(mm[u].y, zz[u][j].x, J.x); J.y = fma(mm[u].y, zz[u][j].y, J.y);
+            }
+    }
+    for (; k < wdt; ++k) {
+        const int32_t e = base + k * 32 + lane;
+        const double2 m = aj[e];
+        const size_t c2 = 2 * (size_t)col[e];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const double2 zc = z[c2 + J0 + j];
+            double2& A = sA[J0 + j];
+            double2& J = sJ[J0 + j];
+            A.x = fma(m.x, zc.x, A.x); A.y = fma(m.x, zc.y, A.y);
+            J.x = fma(m.y, zc.x, J.x); J.y = fma(m.y, zc.y, J.y);
+        }
+    }
+}
+
+// MINB blocks per SM: 2 caps the registers at 128 (a few spilled) so that one
+// thread per row fits the grid; 1 leaves ~200 registers and a warp takes two
+// slices.
+template <int MINB>
+__global__ void __launch_bounds__(kThreads64, MINB) k_step64_pair(PairArgs a) {
+    __shared__ double sm[32 * kRed];
+    __shared__ double red[kRed];
+    const int lane = threadIdx.x & 31;
+    const int warps_per_block = kThreads64 / 32;
+    const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+    const int total_warps = gridDim.x * warps_per_block;
+    const unsigned nb = gridDim.x;
+    const size_t hs = (size_t)2 * a.n_pad;   // length of one pair vector
+    unsigned gen = 0, flip = 0;
+    double2* U[3] = {a.u0, a.u1, a.u2};
+    double2* x = U[1];
+    if (a.stall) {
+        stalled_wait(a.bar + 2, a.status, a.wait_ns);
+        return;
+    }
+
+    for (int step = 0; step < a.n_steps; ++step) {
+        const double cn[2] = {a.cn[step], a.cn[a.n_steps + step]};
+        const double co[2] = {a.co[step], a.co[a.n_steps + step]};
+        const double2* __restrict__ cur = U[step % 3];
+        const double2* __restrict__ prev = U[(step + 2) % 3];
+        x = U[(step + 1) % 3];
+        // ---- phase R (per signal as in k_step64): b, extrapolated x0, r, D^-1, z
+        double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // per signal: rho.re, rho.im, |r|^2, |b|^2
+        const int h = min(step, a.extrapolate);
+        for (int s = gw; s < a.n_slices; s += total_warps) {
+            const int32_t base = a.sl_ptr[s], wdt = a.sl_w[s];
+            double2 sA[2], sJ[2], sB[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) sA[j] = sJ[j] = sB[j] = make_double2(0.0, 0.0);
+            for (int k = 0; k < wdt; ++k) {
+                const int32_t e = base + k * 32 + lane;
+                const size_t c2 = 2 * (size_t)a.col[e];
+                const double2 m = a.aj[e];
+                const double br = a.bre[e];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const double2 uj = cur[c2 + j];
+                    sA[j].x = fma(m.x, uj.x, sA[j].x); sA[j].y = fma(m.x, uj.y, sA[j].y);
+                    sJ[j].x = fma(m.y, uj.x, sJ[j].x); sJ[j].y = fma(m.y, uj.y, sJ[j].y);
+                    sB[j].x = fma(br, uj.x, sB[j].x);  sB[j].y = fma(br, uj.y, sB[j].y);
+                }
+            }
+            const int64_t i = (int64_t)s * 32 + lane;
+            const double dAi = a.dA[i], dJi = a.dJ[i];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const size_t vi = 2 * (size_t)i + j;
+                const double2 b = make_double2(fma(co[j], sJ[j].y, sB[j].x), fma(-co[j], sJ[j].x, sB[j].y));
+                const double2 ui = cur[vi];
+                double2 gA = sA[j], gJ = sJ[j], xi = ui;
+                if (step >= 1 && a.extrapolate > 0) {
+                    const double2 uo = prev[vi], pA = a.pa[vi], pJ = a.pj[vi];
+                    double2* H = a.hd + (size_t)(step & 3) * 3 * hs;
+                    H[vi] = make_double2(ui.x - uo.x, ui.y - uo.y);
+                    H[hs + vi] = make_double2(sA[j].x - pA.x, sA[j].y - pA.y);
+                    H[2 * hs + vi] = make_double2(sJ[j].x - pJ.x, sJ[j].y - pJ.y);
+                }
+                if (a.extrapolate > 0) {
+                    a.pa[vi] = sA[j];
+                    a.pj[vi] = sJ[j];
+                }
+                for (int jj = 1; jj <= h; ++jj) {
+                    const double c = extrap_coef(h, jj);
+                    const double2* H = a.hd + (size_t)((step - jj + 1) & 3) * 3 * hs;
+                    const double2 d = H[vi], dAv = H[hs + vi], dJv = H[2 * hs + vi];
+                    xi.x = fma(c, d.x, xi.x); xi.y = fma(c, d.y, xi.y);
+                    gA.x = fma(c, dAv.x, gA.x); gA.y = fma(c, dAv.y, gA.y);
+                    gJ.x = fma(c, dJv.x, gJ.x); gJ.y = fma(c, dJv.y, gJ.y);
+                }
+                const double2 ax = make_double2(fma(-cn[j], gJ.y, gA.x), fma(cn[j], gJ.x, gA.y));
+                x[vi] = xi;
+                const double2 rr = make_double2(b.x - ax.x, b.y - ax.y);
+                const double2 di = cinv(make_double2(dAi, cn[j] * dJi));
+                const double2 zz = cmul(di, rr);
+                a.dinv[vi] = di;
+                a.r[vi] = rr;
+                a.z[vi] = zz;
+                a.p[vi] = make_double2(0.0, 0.0);
+                a.q[vi] = make_double2(0.0, 0.0);
+                const double2 rz = cmul(rr, zz);
+                acc[4 * j + 0] += rz.x;
+                acc[4 * j + 1] += rz.y;
+                acc[4 * j + 2] += rr.x * rr.x + rr.y * rr.y;
+                acc[4 * j + 3] += b.x * b.x + b.y * b.y;
+            }
+        }
+        if (!reduce_all<8>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
+        double2 rho[2], beta[2];
+        double rr2[2], bb2[2], tol2[2];
+        int it[2] = {0, 0};
+        bool act[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            rho[j] = make_double2(acc[4 * j], acc[4 * j + 1]);
+            rr2[j] = acc[4 * j + 2];
+            bb2[j] = acc[4 * j + 3];
+            tol2[j] = a.rtol2 * bb2[j];
+            beta[j] = make_double2(0.0, 0.0);
+            act[j] = rr2[j] > tol2[j];
+        }
+        bool failed = false;  // uniform across the grid, as every decision below
+        while (act[0] || act[1]) {
+            if ((act[0] && it[0] >= a.maxit) || (act[1] && it[1] >= a.maxit)) {
+                if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_NOT_CONVERGED);
+                failed = true;
+                break;
+            }
+            // ---- phase A: w = A z ; q = w + beta q ; p = z + beta p ; mu = p^T q
+            double mu[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int s = gw; s < a.n_slices; s += total_warps) {
+                const int32_t base = a.sl_ptr[s], wdt = a.sl_w[s];
+                double2 sA[2], sJ[2];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) sA[j] = sJ[j] = make_double2(0.0, 0.0);
+                if (act[0] && act[1])
+                    pair_row_spmv<0, 2>(a.col, a.aj, a.z, base, wdt, lane, sA, sJ);
+                else if (act[0])
+                    pair_row_spmv<0, 1>(a.col, a.aj, a.z, base, wdt, lane, sA, sJ);
+                else
+                    pair_row_spmv<1, 1>(a.col, a.aj, a.z, base, wdt, lane, sA, sJ);
+                const int64_t i = (int64_t)s * 32 + lane;
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    if (!act[j]) continue;
+                    const size_t vi = 2 * (size_t)i + j;
+                    const double2 zi = a.z[vi], pi = a.p[vi], qo = a.q[vi];
+                    const double2 bp = cmul(beta[j], pi), bq = cmul(beta[j], qo);
+                    const double2 pn = make_double2(zi.x + bp.x, zi.y + bp.y);
+                    const double2 qn = make_double2(fma(-cn[j], sJ[j].y, sA[j].x) + bq.x,
+                                                    fma(cn[j], sJ[j].x, sA[j].y) + bq.y);
+                    a.p[vi] = pn;
+                    a.q[vi] = qn;
+                    const double2 pq = cmul(pn, qn);
+                    mu[2 * j] += pq.x;
+                    mu[2 * j + 1] += pq.y;
+                }
+            }
+            if (!reduce_all<4>(mu, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
+            double2 alpha[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                alpha[j] = make_double2(0.0, 0.0);
+                if (!act[j]) continue;
+                const double2 muv = make_double2(mu[2 * j], mu[2 * j + 1]);
+                const double mun = muv.x * muv.x + muv.y * muv.y;
+                if (!(mun > 0.0) || !isfinite(mun)) failed = true;
+                else alpha[j] = cdiv(rho[j], muv);
+            }
+            if (failed) {
+                if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_BREAKDOWN);
+                break;
+            }
+            // ---- phase B: x += alpha p ; r -= alpha q ; z = D^-1 r
+            double acc3[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            for (int s = gw; s < a.n_slices; s += total_warps) {
+                const int64_t i = (int64_t)s * 32 + lane;
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    if (!act[j]) continue;
+                    const size_t vi = 2 * (size_t)i + j;
+                    const double2 pn = a.p[vi], qi = a.q[vi];
+                    double2 xi = x[vi], ri = a.r[vi];
+                    const double2 ap = cmul(alpha[j], pn), aq = cmul(alpha[j], qi);
+                    xi.x += ap.x; xi.y += ap.y;
+                    ri.x -= aq.x; ri.y -= aq.y;
+                    const double2 zi = cmul(a.dinv[vi], ri);
+                    x[vi] = xi;
+                    a.r[vi] = ri;
+                    a.z[vi] = zi;
+                    const double2 rz = cmul(ri, zi);
+                    acc3[3 * j] += rz.x;
+                    acc3[3 * j + 1] += rz.y;
+                    acc3[3 * j + 2] += ri.x * ri.x + ri.y * ri.y;
+                }
+            }
+            if (!reduce_all<6>(acc3, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                if (!act[j]) continue;
+                const double2 rho_new = make_double2(acc3[3 * j], acc3[3 * j + 1]);
+                rr2[j] = acc3[3 * j + 2];
+                ++it[j];
+                const double rhon = rho[j].x * rho[j].x + rho[j].y * rho[j].y;
+                if (!(rhon > 0.0) || !isfinite(rr2[j])) {
+                    if (rr2[j] > tol2[j] || !isfinite(rr2[j])) failed = true;
+                    act[j] = false;
+                    continue;
+                }
+                beta[j] = cdiv(rho_new, rho[j]);
+                rho[j] = rho_new;
+                act[j] = rr2[j] > tol2[j];
+            }
+            if (failed) {
+                if (threadIdx.x == 0) atomicCAS(a.status, DEV_OK, DEV_BREAKDOWN);
+                break;
+            }
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                a.iters[j * a.n_steps + step] = it[j];
+                a.relres[j * a.n_steps + step] = (bb2[j] > 0.0) ? sqrt(rr2[j] / bb2[j]) : sqrt(rr2[j]);
+            }
+        }
+        if (failed) return;
+    }
+    // ---- signals: S_j = sum w Re(u_N,j), per compartment
+    for (int j = 0; j < 2; ++j) {
+        double acc[kRed];
+#pragma unroll
+        for (int k = 0; k < kRed; ++k) acc[k] = 0.0;
+        for (int s = gw; s < a.n_slices; s += total_warps) {
+            const int64_t i = (int64_t)s * 32 + lane;
+            const int c = a.rcomp[i];
+            if (c >= 0) {
+                const double v = a.w[i] * x[2 * (size_t)i + j].x;
+                acc[0] += v;
+#pragma unroll
+                for (int k = 0; k < kMaxCompartments; ++k)
+                    if (k == c) acc[1 + k] += v;
+            }
+        }
+        if (!reduce_all<kRed>(acc, a.partials, nb, flip, a.bar, a.status, gen, sm, red, a.wait_ns)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < kRed; ++k) a.out[j * kRed + k] = acc[k];
+        }
+    }
+}
+
+// Initial state of a pair: both signals start from u0 (or 1); padding rows 0.
+__global__ void k_pair_init(int64_t n, int64_t n_pad, const int32_t* __restrict__ dof_vertex,
+                            const double* __restrict__ u0, double2* __restrict__ x, double2* __restrict__ xprev) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    const double2 v = (i < n) ? make_double2(u0 ? u0[dof_vertex[i]] : 1.0, 0.0) : make_double2(0.0, 0.0);
+    x[2 * i] = v;
+    x[2 * i + 1] = v;
+    xprev[2 * i] = v;
+    xprev[2 * i + 1] = v;
+}
+
+// Final states of a pair, [row][2] -> two [row] vectors.
+__global__ void k_pair_extract(int64_t n_pad, const double2* __restrict__ x, double2* __restrict__ s0,
+                               double2* __restrict__ s1) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    s0[i] = x[2 * i];
+    s1[i] = x[2 * i + 1];
+}
+
 // Pack the SELL values of one signal: {A_re, J_g}, B_re, and the diagonals.
 __global__ void k_pack64(int64_t sell, const int32_t* __restrict__ sl_pos, const double* __restrict__ M,
                          const double* __restrict__ K, const double* __restrict__ T, const double* __restrict__ R,
@@ -491,6 +847,14 @@ static void prepare_fp64(bt_ctx* ctx, Solver64& W) {
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step64, kThreads64, 0));
     BT_REQUIRE(per_sm >= 1, BT_ERR_CUDA, "stepper kernel does not fit on an SM");
     const int need = (m.n_slices + kThreads64 / 32 - 1) / (kThreads64 / 32);
+    // Fewer blocks make the grid-wide reductions (every block sums all block
+    // partials) and barriers cheaper; a warp then takes two or more slices.  On
+    // GB300 one block per SM is faster while the mesh needs at most four blocks
+    // per SM of one thread per row (40^3: 1.19x, 48^3: 1.15x), equal beyond
+    // (64^3, 311 k rows: 0.6 % slower), so "auto" caps there only.
+    const int cap = ctx->opt_fp64_blocks_per_sm > 0 ? ctx->opt_fp64_blocks_per_sm
+                    : (ctx->opt_fp64_blocks_per_sm < 0 && need <= 4 * ctx->num_sms) ? 1 : 0;
+    if (cap > 0) per_sm = std::min(per_sm, cap);
     W.nblocks = std::max(1, std::min(per_sm * ctx->num_sms, need));
     W.partials.alloc((size_t)2 * W.nblocks * kRed);
 }
@@ -587,6 +951,89 @@ static float run_steps_fp64(bt_ctx* ctx, Solver64& W, const double* d_cn, const 
     return ms;
 }
 
+// The paired kernel of option fp64.pair_signals: 1 = two blocks per SM, 2 = one.
+static const void* pair_kernel(const bt_ctx* ctx) {
+    return ctx->opt_fp64_pair == 2 ? (const void*)k_step64_pair<1> : (const void*)k_step64_pair<2>;
+}
+
+// Workspace of k_step64_pair (allocated on first use, kept across solves of one size).
+static void prepare_pair(bt_ctx* ctx, Solver64& W) {
+    const size_t n2 = (size_t)2 * W.n_pad;
+    const size_t ns2 = (size_t)2 * ctx->sched.n_steps;
+    for (auto* v : {&W.pu[0], &W.pu[1], &W.pu[2], &W.pr, &W.pz, &W.pp, &W.pq, &W.pdinv, &W.ppa, &W.ppj})
+        v->alloc(n2);
+    W.phd.alloc(12 * n2);
+    W.pcn.alloc(ns2);
+    W.pco.alloc(ns2);
+    W.prelres.alloc(ns2);
+    W.piters.alloc(ns2);
+    W.pout.alloc(2 * kRed);
+    int per_sm = 0;
+    BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pair_kernel(ctx), kThreads64, 0));
+    BT_REQUIRE(per_sm >= 1, BT_ERR_CUDA, "paired stepper kernel does not fit on an SM");
+    W.pair_variant = ctx->opt_fp64_pair;
+    const int need = (ctx->mesh.n_slices + kThreads64 / 32 - 1) / (kThreads64 / 32);
+    W.pair_blocks = std::max(1, std::min(per_sm * ctx->num_sms, need));
+    W.ppartials.alloc((size_t)2 * W.pair_blocks * kRed);
+}
+
+// One cooperative launch of k_step64_pair over the whole schedule for the two
+// signals whose schedules are in W.pcn / W.pco (signal j at [j * n_steps]); the
+// matrix and row data are those of pack_signal_fp64.  Returns the device time.
+static float run_pair_fp64(bt_ctx* ctx, Solver64& W, const double* d_u0, double rtol, int maxit,
+                           std::vector<int32_t>& iters, std::vector<double>& relres, double* out) {
+    Mesh& m = ctx->mesh;
+    cudaStream_t s = ctx->stream;
+    const int n_steps = ctx->sched.n_steps;
+    k_pair_init<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(m.n_dofs, W.n_pad, m.dof_vertex, d_u0,
+                                                                   W.pu[0], W.pu[2]);
+    BT_CUDA(cudaGetLastError());
+    W.bar.zero(s);
+    W.status.zero(s);
+    PairArgs a;
+    a.n_slices = m.n_slices;
+    a.sl_ptr = m.sl_ptr; a.sl_w = m.sl_w; a.col = m.sl_col;
+    a.aj = W.aj; a.bre = W.bre; a.dA = W.dA; a.dJ = W.dJ; a.w = W.w; a.rcomp = W.rcomp;
+    a.u0 = W.pu[0]; a.u1 = W.pu[1]; a.u2 = W.pu[2];
+    a.r = W.pr; a.z = W.pz; a.p = W.pp; a.q = W.pq; a.dinv = W.pdinv;
+    a.pa = W.ppa; a.pj = W.ppj; a.hd = W.phd;
+    a.partials = W.ppartials; a.bar = W.bar; a.status = W.status;
+    a.cn = W.pcn; a.co = W.pco;
+    a.n_steps = n_steps;
+    a.maxit = maxit;
+    a.extrapolate = ctx->opt_fp64_extrapolate != 0 ? std::max(1, std::min(4, ctx->opt_fp64_extrapolate)) : 0;
+    a.rtol2 = rtol * rtol;
+    a.n_pad = W.n_pad;
+    a.iters = W.piters; a.relres = W.prelres; a.out = W.pout;
+    a.wait_ns = ctx->opt_wait_ns;
+    a.stall = ctx->opt_stall_first_wait;
+    {
+        const void* need_ptrs[] = {a.sl_ptr, a.sl_w, a.col, a.aj, a.bre, a.dA, a.dJ, a.w, a.rcomp, a.u0, a.u1,
+                                   a.u2, a.r, a.z, a.p, a.q, a.dinv, a.pa, a.pj, a.hd, a.partials, a.bar,
+                                   a.status, a.cn, a.co, a.iters, a.relres, a.out};
+        for (const void* ptr : need_ptrs)
+            BT_REQUIRE(ptr != nullptr, BT_ERR_STATE, "paired stepper: a device buffer is not allocated");
+        BT_REQUIRE(n_steps >= 1 && W.pcn.n == (size_t)2 * n_steps && W.piters.n == (size_t)2 * n_steps,
+                   BT_ERR_STATE, "paired stepper: schedule size mismatch");
+    }
+    void* args[] = {&a};
+    BT_CUDA(cudaEventRecord(ctx->ev1, s));
+    BT_CUDA(cudaLaunchCooperativeKernel(pair_kernel(ctx), dim3(W.pair_blocks), dim3(kThreads64), args, 0, s));
+    BT_CUDA(cudaEventRecord(ctx->ev2, s));
+    int hst = 0;
+    BT_CUDA(cudaMemcpyAsync(&hst, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    iters.resize((size_t)2 * n_steps);
+    relres.resize((size_t)2 * n_steps);
+    W.piters.download(iters.data(), iters.size(), s);
+    W.prelres.download(relres.data(), relres.size(), s);
+    W.pout.download(out, 2 * kRed, s);
+    BT_CUDA(cudaStreamSynchronize(s));
+    map_status(hst);
+    float ms = 0.0f;
+    BT_CUDA(cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2));
+    return ms;
+}
+
 static void schedule_row(const Schedule& S, int32_t row, double q, std::vector<double>& hcn,
                          std::vector<double>& hco) {
     BT_REQUIRE(row >= 0 && row < S.n_seq, BT_ERR_INVALID, "sequence index out of range");
@@ -626,8 +1073,48 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
         st->stepper_ms = 0.0;
     }
     float stepper_ms_total = 0.0f;
+    auto record = [&](int32_t sg, const double* out, const int32_t* it, const double* res) {
+        sig[sg] = out[0];
+        if (comp_sig)
+            for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)sg * m.n_comp + c] = out[1 + c];
+        for (int k = 0; k < S.n_steps; ++k) {
+            ctx->last_iters[(size_t)sg * S.n_steps + k] = it[k];
+            if (st) {
+                st->max_iterations = std::max(st->max_iterations, it[k]);
+                st->total_iterations += it[k];
+                st->max_rel_residual = std::max(st->max_rel_residual, res[k]);
+            }
+        }
+    };
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
     for (int32_t sg = 0; sg < nsig; ++sg) {
+        // two consecutive signals of one direction share a k_step64_pair launch
+        const double* g0 = gdir + 3 * sg;
+        if (ctx->opt_fp64_pair && !ctx->per.on && sg + 1 < nsig && g0[0] == g0[3] && g0[1] == g0[4] &&
+            g0[2] == g0[5]) {
+            if (!W.pair_blocks || W.pair_variant != ctx->opt_fp64_pair || W.pcn.n != (size_t)2 * S.n_steps)
+                prepare_pair(ctx, W);
+            std::vector<double> hcn2, hco2, pout(2 * kRed), pres;
+            std::vector<int32_t> pit;
+            for (int j = 0; j < 2; ++j) {
+                schedule_row(S, seq ? seq[sg + j] : 0, q[sg + j], hcn, hco);
+                hcn2.insert(hcn2.end(), hcn.begin(), hcn.end());
+                hco2.insert(hco2.end(), hco.begin(), hco.end());
+            }
+            W.pcn.upload(hcn2.data(), hcn2.size(), s);
+            W.pco.upload(hco2.data(), hco2.size(), s);
+            pack_signal_fp64(ctx, W, g0, u0 ? d_u0.p : nullptr);
+            stepper_ms_total += run_pair_fp64(ctx, W, u0 ? d_u0.p : nullptr, rtol, maxit, pit, pres, pout.data());
+            k_pair_extract<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(
+                W.n_pad, W.pu[S.n_steps % 3], W.saved.p + (size_t)sg * W.n_pad, W.saved.p + (size_t)(sg + 1) * W.n_pad);
+            BT_CUDA(cudaGetLastError());
+            for (int j = 0; j < 2; ++j)
+                record(sg + j, pout.data() + j * kRed, pit.data() + (size_t)j * S.n_steps,
+                       pres.data() + (size_t)j * S.n_steps);
+            if (st) st->kernel_launches += 5;
+            ++sg;
+            continue;
+        }
         schedule_row(S, seq ? seq[sg] : 0, q[sg], hcn, hco);
         W.cn.upload(hcn.data(), S.n_steps, s);
         W.co.upload(hco.data(), S.n_steps, s);
@@ -643,17 +1130,7 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
                                            nullptr, 1, rtol, maxit, &hit, &hres, hout.data());
         BT_CUDA(cudaMemcpyAsync(W.saved.p + (size_t)sg * W.n_pad, W.u[S.n_steps % 3].p,
                                 W.n_pad * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        sig[sg] = hout[0];
-        if (comp_sig)
-            for (int c = 0; c < m.n_comp; ++c) comp_sig[(size_t)sg * m.n_comp + c] = hout[1 + c];
-        for (int k = 0; k < S.n_steps; ++k) {
-            ctx->last_iters[(size_t)sg * S.n_steps + k] = hit[k];
-            if (st) {
-                st->max_iterations = std::max(st->max_iterations, hit[k]);
-                st->total_iterations += hit[k];
-                st->max_rel_residual = std::max(st->max_rel_residual, hres[k]);
-            }
-        }
+        record(sg, hout.data(), hit.data(), hres.data());
         if (st) st->kernel_launches += 3;
     }
     BT_CUDA(cudaEventRecord(ctx->ev2, s));
