@@ -847,11 +847,13 @@ static void prepare_fp64(bt_ctx* ctx, Solver64& W) {
     BT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step64, kThreads64, 0));
     BT_REQUIRE(per_sm >= 1, BT_ERR_CUDA, "stepper kernel does not fit on an SM");
     const int need = (m.n_slices + kThreads64 / 32 - 1) / (kThreads64 / 32);
-    // Fewer blocks make the grid-wide reductions (every block sums all block
-    // partials) and barriers cheaper; a warp then takes two or more slices.  On
-    // GB300 one block per SM is faster while the mesh needs at most four blocks
-    // per SM of one thread per row (40^3: 1.19x, 48^3: 1.15x), equal beyond
-    // (64^3, 311 k rows: 0.6 % slower), so "auto" caps there only.
+    // With fewer blocks a warp takes two or more slices and each grid barrier
+    // has fewer arrivals and pollers.  On GB300 one block per SM is faster
+    // while the mesh needs at most four blocks per SM of one thread per row
+    // (40^3: 1.19x, 48^3: 1.15x), equal beyond (64^3, 311 k rows: 0.6 %
+    // slower), so "auto" caps there only.  (Loading the block partials of a
+    // grid sum with all threads of a block instead of one warp was 1.3 %
+    // slower: the gain is not in the partial sums.)
     const int cap = ctx->opt_fp64_blocks_per_sm > 0 ? ctx->opt_fp64_blocks_per_sm
                     : (ctx->opt_fp64_blocks_per_sm < 0 && need <= 4 * ctx->num_sms) ? 1 : 0;
     if (cap > 0) per_sm = std::min(per_sm, cap);
