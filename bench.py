@@ -310,9 +310,11 @@ def roofline_fp64(info, st, its, peak, peak_src, traffic):
         out["note"] = ("L2-resident: ncu counts %.0f MB of DRAM traffic per launch of %s, %.3f%% of the %.0f GB "
                        "of algorithmic bytes, so `achieved` counts L2-served bytes and `frac` is not an HBM "
                        "fraction; the stepper is bound by the FP64 pipe (GB300 runs FP64 at a small fraction of "
-                       "FP32; profiles/k_step64_cfg2.md)"
+                       "FP32; %s)"
                        % (traffic["bytes_per_launch"] / 1e6, traffic.get("kernel", "the stepper"),
-                          100.0 * traffic["bytes_per_launch"] / byts, byts / 1e9))
+                          100.0 * traffic["bytes_per_launch"] / byts, byts / 1e9,
+                          "profiles/k_step64_pair_cfg2.md: FP64 pipe active 61.6% of peak" if paired
+                          else "profiles/k_step64_cfg2.md: FP64 pipe active 59% of peak"))
     else:
         out["note"] = "no DRAM capture for this workload"
     return out
