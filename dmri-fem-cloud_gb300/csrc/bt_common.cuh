@@ -210,7 +210,7 @@ struct bt_ctx {
     int opt_mixed_reduce = -1;
     double opt_mixed_growth2 = 1e8;   // divergence guard of a sweep (squared-norm growth over its minimum)
     int opt_fp64_extrapolate = 4;    // order of the FP64 path's extrapolated initial guess (0..4)
-    int opt_fp64_pair = 2;            // FP64 path: two consecutive signals of one direction share a launch
+    int opt_fp64_pair = 2;            // FP64 path: two signals of one direction share a launch (0: off)
     int opt_fp64_blocks_per_sm = -1;  // FP64 one-signal stepper: blocks per SM cap (0: as many as fit, -1: auto)
     int opt_mixed_inner = 2;          // grid-wide reductions per inner COCG iteration: 1 or 2
     int opt_mixed_sort = 1;           // order a solve's signals by (sequence, |q|) before batching

@@ -1088,33 +1088,50 @@ void solve_fp64(bt_ctx* ctx, int32_t nsig, const double* q, const double* gdir, 
             }
         }
     };
+    // Two signals of one direction (identical gdir rows) share a k_step64_pair
+    // launch: each signal is paired with the next unpaired signal of its
+    // direction; outputs keep the call's order.
+    std::vector<int32_t> mate(nsig, -1);
+    if (ctx->opt_fp64_pair && !ctx->per.on) {
+        for (int32_t i = 0; i < nsig; ++i) {
+            if (mate[i] != -1) continue;
+            const double* gi = gdir + 3 * i;
+            for (int32_t j = i + 1; j < nsig; ++j) {
+                const double* gj = gdir + 3 * j;
+                if (mate[j] == -1 && gi[0] == gj[0] && gi[1] == gj[1] && gi[2] == gj[2]) {
+                    mate[i] = j;
+                    mate[j] = i;
+                    break;
+                }
+            }
+        }
+    }
     BT_CUDA(cudaEventRecord(ctx->ev0, s));
     for (int32_t sg = 0; sg < nsig; ++sg) {
-        // two consecutive signals of one direction share a k_step64_pair launch
-        const double* g0 = gdir + 3 * sg;
-        if (ctx->opt_fp64_pair && !ctx->per.on && sg + 1 < nsig && g0[0] == g0[3] && g0[1] == g0[4] &&
-            g0[2] == g0[5]) {
+        if (mate[sg] >= 0 && mate[sg] < sg) continue;   // stepped with its earlier partner
+        if (mate[sg] > sg) {
+            const int32_t idx[2] = {sg, mate[sg]};
             if (!W.pair_blocks || W.pair_variant != ctx->opt_fp64_pair || W.pcn.n != (size_t)2 * S.n_steps)
                 prepare_pair(ctx, W);
             std::vector<double> hcn2, hco2, pout(2 * kRed), pres;
             std::vector<int32_t> pit;
             for (int j = 0; j < 2; ++j) {
-                schedule_row(S, seq ? seq[sg + j] : 0, q[sg + j], hcn, hco);
+                schedule_row(S, seq ? seq[idx[j]] : 0, q[idx[j]], hcn, hco);
                 hcn2.insert(hcn2.end(), hcn.begin(), hcn.end());
                 hco2.insert(hco2.end(), hco.begin(), hco.end());
             }
             W.pcn.upload(hcn2.data(), hcn2.size(), s);
             W.pco.upload(hco2.data(), hco2.size(), s);
-            pack_signal_fp64(ctx, W, g0, u0 ? d_u0.p : nullptr);
+            pack_signal_fp64(ctx, W, gdir + 3 * sg, u0 ? d_u0.p : nullptr);
             stepper_ms_total += run_pair_fp64(ctx, W, u0 ? d_u0.p : nullptr, rtol, maxit, pit, pres, pout.data());
             k_pair_extract<<<(unsigned)((W.n_pad + 255) / 256), 256, 0, s>>>(
-                W.n_pad, W.pu[S.n_steps % 3], W.saved.p + (size_t)sg * W.n_pad, W.saved.p + (size_t)(sg + 1) * W.n_pad);
+                W.n_pad, W.pu[S.n_steps % 3], W.saved.p + (size_t)idx[0] * W.n_pad,
+                W.saved.p + (size_t)idx[1] * W.n_pad);
             BT_CUDA(cudaGetLastError());
             for (int j = 0; j < 2; ++j)
-                record(sg + j, pout.data() + j * kRed, pit.data() + (size_t)j * S.n_steps,
+                record(idx[j], pout.data() + j * kRed, pit.data() + (size_t)j * S.n_steps,
                        pres.data() + (size_t)j * S.n_steps);
             if (st) st->kernel_launches += 5;
-            ++sg;
             continue;
         }
         schedule_row(S, seq ? seq[sg] : 0, q[sg], hcn, hco);

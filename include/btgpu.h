@@ -383,8 +383,9 @@ int bt_tangent(bt_ctx* ctx, double q, const double* gdir, int32_t sequence, cons
  *   "fp64.extrapolate"      order of the FP64 path's initial guess, extrapolated in time from the
  *                           last states: 4 (default), 3, 2, 1 (2 u_n - u_{n-1}) or 0 (u_n); the strong
  *                           pseudo-periodic stepper uses 2 u_n - u_{n-1} for any order >= 1
- *   "fp64.pair_signals"     2 (default) or 1: bt_solve's FP64 path steps two consecutive signals of
- *                           one gradient direction in one launch (shared matrix loads and grid
+ *   "fp64.pair_signals"     2 (default) or 1: bt_solve's FP64 path steps two signals of one gradient
+ *                           direction (identical gdir rows; each signal is paired with the next
+ *                           unpaired one of its direction) in one launch (shared matrix loads and grid
  *                           barriers, each signal with its own COCG scalars and stopping test); 2
  *                           runs one block per SM (~200 registers), 1 two blocks per SM (128
  *                           registers, a few spilled); 0: one launch per signal.  Not used with

@@ -75,6 +75,27 @@ def test_pair_matches_single_launches(pkg, lib, mode):
     ctx.close()
 
 
+def test_pair_interleaved_directions(pkg, lib):
+    """Directions A, B, A, B, A: signals 0 and 2, 1 and 3 are paired across the
+    positions (4 runs alone); outputs stay in the call's order."""
+    w = pkg.meshgen.workload("cfg3", n=10)
+    ctx = _ctx(pkg, w)
+    q, g, seq = _signals(pkg, w, [0, 9, 2, 11, 4])
+    assert not np.array_equal(g[0], g[1])
+    g[2] = g[4] = g[0]
+    g[3] = g[1]
+    ref, ref_u, ref_it = _run(ctx, 0, q, g, seq)
+    got, got_u, got_it = _run(ctx, 2, q, g, seq)
+    assert got["stats"]["kernel_launches"] == 5 + 5 + 3
+    rel = np.abs(got["signal"] - ref["signal"]) / np.abs(ref["signal"])
+    assert rel.max() <= PAIR_RTOL, rel
+    for k in range(len(q)):
+        err = np.abs(got_u[k] - ref_u[k]).max() / np.abs(ref_u[k]).max()
+        assert err <= 1e-11, (k, err)
+    assert np.abs(got_it - ref_it).max() <= 1
+    ctx.close()
+
+
 def test_pair_initial_condition_and_golden(pkg, lib, golden):
     """A non-unit initial condition through both forms, and the full-size
     two-compartment fixture through the pair (its signals share a direction)."""
